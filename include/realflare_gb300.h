@@ -1,0 +1,225 @@
+/*
+ * realflare_gb300 — C ABI of the GB300 flare render path.
+ *
+ * Every entry point takes plain device pointers (allocated and owned by the caller), sizes
+ * and a CUDA stream handle (cudaStream_t passed as void*; NULL = legacy default stream).
+ * Work is enqueued asynchronously on that stream; nothing is allocated inside the library
+ * except where a function says so. Every function returns an rf_status; there are no
+ * exceptions across the ABI. Device pointers must be 16-byte aligned.
+ *
+ * Each declaration names the reference interface it replaces (paths inside the
+ * beatreichenbach/realflare project, v0.6.4).
+ */
+#ifndef REALFLARE_GB300_H
+#define REALFLARE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RF_LAMBDA_MIN 390 /* realflare/api/tasks/opencl.py:14 */
+#define RF_LAMBDA_MAX 730 /* realflare/api/tasks/opencl.py:15 */
+#define RF_LAMBDA_MID 560 /* realflare/api/tasks/opencl.py:16 */
+#define RF_BATCH_PRIMITIVE_COUNT 255 /* realflare/api/tasks/rasterizing.py:26 */
+#define RF_RAY_PLANES 6  /* pos.x, pos.y, pos_apt.x, pos_apt.y, rrel, reflectance */
+#define RF_VERTEX_FLOATS 8 /* pos.xy, uv.xy, rrel, reflectance, intensity, pad */
+#define RF_SPECTRUM_WIDTH 340 /* CIE rows 390..729 nm */
+
+typedef enum rf_status {
+    RF_OK = 0,
+    RF_ERR_INVALID_ARG = 1,     /* a size, pointer or setting outside the supported range */
+    RF_ERR_OUT_OF_MEMORY = 2,   /* a device allocation requested by the caller failed */
+    RF_ERR_TIMEOUT = 3,         /* a bounded device wait gave up (device error flag set) */
+    RF_ERR_CUDA = 4,            /* a CUDA runtime call failed (see rf_last_cuda_error) */
+    RF_ERR_WORKSPACE = 5,       /* workspace too small; the required size was written back */
+    RF_ERR_NOT_SUPPORTED = 6    /* e.g. a non-power-of-two FFT size */
+} rf_status;
+
+/* One lens element (64 bytes). radius/ior/height/center/coating/coefficients carry the
+ * meaning of the reference's lens_element_dtype (realflare/api/tasks/opencl.py:28-37,
+ * filled by realflare/api/lens.py:40-86). coating_layers selects the coating model at a
+ * reflection: 0 = the reference's single-layer quarter-wave rule (lambda0 = coating nm,
+ * thickness lambda0 / (4 nc), realflare/api/tasks/cl/raytracing.cl:316-335); 1 = the same
+ * single-layer formula with thickness coating_thickness[0] nm; 2 = an exact two-layer
+ * thin-film stack with thicknesses coating_thickness[0..1] nm and layer indices
+ * rf_trace_args.coating_layer_ior. coefficients[0..5] = Sellmeier B1,C1,B2,C2,B3,C3;
+ * coefficients[0] = NaN on element 0 turns dispersion off. */
+typedef struct rf_lens_element {
+    float radius;
+    float ior;
+    float height;
+    float center;
+    int32_t coating;
+    int32_t coating_layers;
+    float coating_thickness[2];
+    float coefficients[8];
+} rf_lens_element;
+
+typedef struct rf_trace_args {
+    int32_t element_count;   /* lens elements including the appended sensor */
+    int32_t aperture_index;
+    int32_t path_count;
+    int32_t wavelength_count;
+    int32_t grid_count;
+    float grid_length;
+    float coating_min_ior;
+    float coating_layer_ior[2];
+    float direction[4];      /* realflare/api/tasks/raytracing.py:92-106 */
+} rf_trace_args;
+
+typedef struct rf_raster_args {
+    int32_t width, height;
+    int32_t bin_size;        /* the reference's BIN_SIZE (realflare/api/data.py:222) */
+    int32_t tile_size;       /* raster tile edge in pixels; must divide bin_size; 0 = auto */
+    int32_t path_count, wavelength_count, wavelength_sub_count, grid_count;
+    int32_t sub_steps;       /* anti-aliasing 1, 2, 4 or 8 */
+    float screen_transform;  /* realflare/api/tasks/rasterizing.py:158-167 */
+    float intensity;         /* light intensity * 1e3 (rasterizing.py:415) */
+    float ghost_scale;       /* 1 - fstop / 32 (rasterizing.py:393) */
+    int32_t ghost_width, ghost_height;
+} rf_raster_args;
+
+/* ---- library ---------------------------------------------------------------------- */
+const char* rf_version(void);
+/* Text of the last CUDA error seen by this thread (empty if none). */
+const char* rf_last_cuda_error(void);
+
+/* ---- ray trace ---------------------------------------------------------------------- */
+/* Replaces RaytracingTask.raytrace's kernel launch (realflare/api/tasks/raytracing.py:
+ * 140-221) and the raytrace kernel (realflare/api/tasks/cl/raytracing.cl:218-359).
+ * elements: device rf_lens_element[element_count]; paths: device int32 pairs [path_count]
+ * (bounce1, bounce2); wavelengths: device float nm [wavelength_count]; rays: device
+ * float[RF_RAY_PLANES][path_count][wavelength_count][grid_count^2] (plane-major). Invalid
+ * rays carry reflectance NaN and the state they had when they stopped. */
+int rf_trace(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
+             const rf_trace_args* args, float* rays, void* stream);
+
+/* ---- quad setup ------------------------------------------------------------------- */
+/* Replaces the prim_shader kernel (realflare/api/tasks/cl/rasterizing.cl:233-320) and its
+ * launch (realflare/api/tasks/rasterizing.py:210-221,321-344). bounds: device float4
+ * [path_count][quads] in mm (x = NaN: culled); intensities: device float
+ * [path_count][quads][wavelength_count]; entries after a degenerate wavelength are 0. */
+int rf_quad_setup(const float* rays, int32_t path_count, int32_t wavelength_count,
+                  int32_t grid_count, float area_orig, float min_area, float* bounds,
+                  float* intensities, void* stream);
+
+/* Replaces the vertex_shader kernel (realflare/api/tasks/cl/rasterizing.cl:322-386) and
+ * its launch (realflare/api/tasks/rasterizing.py:223-235,348-362). vertexes: device
+ * float[path_count * grid_count^2 * wavelength_count + 1][RF_VERTEX_FLOATS] in the
+ * reference's (path, ray, wavelength) order; the extra trailing vertex is zero. Invalid
+ * rays give reflectance NaN and zero elsewhere. */
+int rf_vertex(const float* rays, const float* intensities, int32_t path_count,
+              int32_t wavelength_count, int32_t grid_count, float screen_transform,
+              int32_t width, int32_t height, float* vertexes, void* stream);
+
+/* ---- binning ------------------------------------------------------------------------ */
+/* Reference-layout bin masks: replaces the binner kernel (realflare/api/tasks/cl/
+ * rasterizing.cl:388-469) and its launch (realflare/api/tasks/rasterizing.py:237-255,
+ * 366-385). masks: device uint64[bin_count][batch_count][4], zeroed by this call, with
+ * bit (i+1) of (bin, batch) set when primitive batch*255+i overlaps the bin and bit 0 set
+ * when any is. Used for parity checks and by callers that consume the reference layout. */
+int rf_bin_masks(const float* bounds, int32_t prim_count, float screen_transform,
+                 int32_t width, int32_t height, int32_t bin_size, uint64_t* masks,
+                 void* stream);
+
+/* Scratch bytes rf_bin_tiles needs for prim_count primitives, a pair capacity and the
+ * tile grid of args (width, height, bin_size, tile_size). */
+int rf_bin_workspace_size(int32_t prim_count, int64_t pair_capacity, const rf_raster_args* args,
+                          size_t* bytes);
+
+/* Ordered per-tile primitive lists: for every raster tile, the indices of the primitives
+ * whose reference bin (bin_size) contains the tile and whose conservative pixel bounds
+ * touch it, in increasing primitive order. tile_offsets: device uint32[tiles + 1];
+ * tile_prims: device uint32[pair_capacity]. The pair count is copied to the host
+ * (one stream synchronisation); if it exceeds pair_capacity the call returns
+ * RF_ERR_WORKSPACE and writes the count to *pair_count without filling the lists. */
+int rf_bin_tiles(const float* bounds, int32_t prim_count, const rf_raster_args* args,
+                 void* workspace, size_t workspace_bytes, uint32_t* tile_offsets,
+                 uint32_t* tile_prims, int64_t pair_capacity, int64_t* pair_count, void* stream);
+
+/* ---- raster ------------------------------------------------------------------------- */
+/* Replaces the rasterizer kernel (realflare/api/tasks/cl/rasterizing.cl:524-663), its
+ * launch with the preceding image clear (realflare/api/tasks/rasterizing.py:257-285,
+ * 387-418) and fragment_shader / xyz_to_ap1 (rasterizing.cl:471-522, color.cl:3-10).
+ * ghost: device float[ghost_height][ghost_width]; spectrum: device float[340][4] (CIE XYZ0
+ * 390..729 nm); image: device float[height][width][4] RGBA (AP1, alpha 0, row 0 = top). */
+int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_prims,
+              const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
+              void* stream);
+
+/* Reference-order rasteriser over reference-layout masks (for parity checks). */
+int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_count,
+                    const float* ghost, const float* spectrum, const rf_raster_args* args,
+                    float* image, void* stream);
+
+/* ---- diffraction ------------------------------------------------------------------ */
+/* In-place 2-D FFT of a batch of complex64 images [batch][height][width] (interleaved
+ * re, im), width and height powers of two in [2, 4096]. direction -1 = forward
+ * (exp(-i...)), +1 = inverse; scale multiplies the result (1/sqrt(wh) = numpy "ortho").
+ * Replaces numpy.fft.fft2/fftn/ifftn in realflare/api/tasks/starburst.py:71 and
+ * realflare/utils/frft.py:27-60. scratch: device complex64 buffer of the same size. */
+int rf_fft2(float* data, float* scratch, int32_t batch, int32_t width, int32_t height,
+            int32_t direction, float scale, void* stream);
+
+/* Starburst power spectrum: |fftshift(fft2(A * exp(i pi (x^2+y^2) / (lambda d))))|^2 per
+ * wavelength (realflare/api/tasks/starburst.py:45-81). aperture: device float[h][w];
+ * lambdas_mm: host float[count]; spectrum: device float[count][h][w]; scratch: device
+ * complex64[2][count][h][w]. distance_mm = max(1e-9, distance_m * 1e3). */
+int rf_starburst_spectrum(const float* aperture, int32_t width, int32_t height,
+                          const float* lambdas_mm, int32_t count, float distance_mm,
+                          float* scratch, float* spectrum, void* stream);
+
+typedef struct rf_starburst_args {
+    int32_t width, height;           /* output image */
+    int32_t spectrum_width, spectrum_height, spectrum_count;
+    int32_t samples;
+    float blur, rotation, rotation_weight;
+    float vignetting[2];             /* NaN = off */
+    float intensity;                 /* starburst intensity * 1e-6 */
+    float offset[2], scale[2];
+    float lambda_first, lambda_step; /* per-wavelength spectra: nm of spectrum 0 and step */
+} rf_starburst_args;
+
+/* Replaces the starburst kernel (realflare/api/tasks/cl/starburst.cl:1-87) and its launch
+ * (realflare/api/tasks/starburst.py:83-153). spectrum_count 1 = the reference's single
+ * 560 nm spectrum; > 1 = one spectrum per wavelength (nearest is sampled). image: device
+ * float[height][width][4]. */
+int rf_starburst(const float* spectrum, const float* light_spectrum, const rf_starburst_args* args,
+                 float* image, void* stream);
+
+/* Fractional Fourier transform ghost texture (realflare/api/tasks/ghost.py:13-36 with
+ * realflare/utils/frft.py:20-62): |fftshift(frft(fftshift(A), alpha))| * sqrt(w h).
+ * aperture: device float[h][w]; texture: device float[h][w]; scratch: device
+ * complex64[3][h][w]. */
+int rf_ghost_frft(const float* aperture, int32_t width, int32_t height, float alpha,
+                  float* scratch, float* texture, void* stream);
+
+/* ---- aperture masks ----------------------------------------------------------------- */
+/* aperture_shape kernel (realflare/api/tasks/cl/aperture.cl:5-47): writes image[h][w]. */
+int rf_aperture_shape(float* image, int32_t width, int32_t height, float size_x, float size_y,
+                      int32_t blades, float rotation, float roundness, float softness,
+                      void* stream);
+/* aperture_dust kernel (realflare/api/tasks/cl/aperture.cl:139-174): multiplies image. */
+int rf_aperture_dust(float* image, int32_t width, int32_t height, float size_x, float size_y,
+                     float strength, float density, float radius, float parallax_x,
+                     float parallax_y, float softness, void* stream);
+/* Blurred-noise dust (no reference counterpart): image *= 1 - strength * G_sigma * noise,
+ * a separable Gaussian of radius ceil(4 sigma), clamp-to-edge. noise: device float[h][w];
+ * scratch: device float[h][w]. */
+int rf_aperture_noise_dust(float* image, const float* noise, float* scratch, int32_t width,
+                           int32_t height, float strength, float sigma, void* stream);
+
+/* ---- compositing ---------------------------------------------------------------------- */
+/* out = a * wa + b * wb elementwise over n floats (Engine.flare_starburst,
+ * realflare/api/engine.py:174-187, uses wa = 2, wb = 1). */
+int rf_axpby(const float* a, float wa, const float* b, float wb, float* out, int64_t n,
+             void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REALFLARE_GB300_H */

@@ -1,0 +1,97 @@
+"""Host-side argument preparation for the render path.
+
+Restates the host halves of ``RaytracingTask.raytrace`` (``realflare/api/tasks/raytracing.py:
+140-221``) and ``RasterizingTask.rasterize`` (``realflare/api/tasks/rasterizing.py:296-421``):
+lens elements, ghost paths, wavelengths and light direction for the trace; screen transform,
+quad area, bin sizes and scale factors for the raster.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lens as lens_mod
+from ._abi import RasterArgs, TraceArgs
+from .data import Project, RealflareError
+
+
+@dataclass
+class TraceInputs:
+    elements: np.ndarray      # rf_lens_element[E]
+    paths: np.ndarray         # int32 [P, 2]
+    wavelengths: np.ndarray   # float32 [W]
+    args: TraceArgs
+
+    @property
+    def ray_count(self) -> int:
+        return self.args.path_count * self.args.wavelength_count * self.args.grid_count**2
+
+
+def trace_inputs(project: Project, paths=None, path_indexes: tuple = ()) -> TraceInputs | None:
+    """Inputs of one trace; None when the lens has fewer than two elements
+    (``raytracing.py:164-165``). ``paths`` overrides the reference's ``ray_paths``."""
+    lens = project.flare.lens
+    model = lens_mod.resolve_model(lens)
+    sensor_size = (lens.sensor_size.width(), lens.sensor_size.height())
+    elements = lens_mod.elements(
+        model, sensor_size, lens.glasses_path, lens.abbe_nr_adjustment, tuple(lens.coating),
+        tuple(lens.coating_thickness),
+    )
+    if len(elements) <= 1:
+        return None
+    if paths is None:
+        paths = lens_mod.ray_paths(model, tuple(path_indexes))
+    paths = np.asarray(paths, np.int32).reshape(-1, 2)
+    wavelengths = lens_mod.render_wavelengths(project.render)
+    render = project.render
+    light = project.flare.light
+    direction = lens_mod.direction(
+        (light.position.x(), light.position.y()), render.resolution, sensor_size, model.focal_length
+    )
+    a = TraceArgs()
+    a.element_count = len(elements)
+    a.aperture_index = model.aperture_index
+    a.path_count = len(paths)
+    a.wavelength_count = len(wavelengths)
+    a.grid_count = render.grid_count
+    a.grid_length = render.grid_length
+    a.coating_min_ior = lens.coating_min_ior
+    a.coating_layer_ior[0] = lens.coating_layer_ior[0]
+    a.coating_layer_ior[1] = lens.coating_layer_ior[1]
+    for i in range(4):
+        a.direction[i] = float(direction[i])
+    if a.grid_count < 2:
+        raise RealflareError('grid_count must be >= 2')
+    return TraceInputs(elements, paths, wavelengths, a)
+
+
+def raster_args(project: Project, path_count: int, wavelength_count: int, ghost_shape: tuple,
+                tile_size: int = 0) -> RasterArgs:
+    render = project.render
+    lens = project.flare.lens
+    sensor_size = (lens.sensor_size.width(), lens.sensor_size.height())
+    a = RasterArgs()
+    a.width = render.resolution.width()
+    a.height = render.resolution.height()
+    a.bin_size = max(render.bin_size, 1)
+    a.tile_size = tile_size
+    a.path_count = path_count
+    a.wavelength_count = wavelength_count
+    # rasterizing.py:390-392: sub-wavelengths only with more than one wavelength
+    a.wavelength_sub_count = render.wavelength_sub_count if wavelength_count > 1 else 1
+    a.grid_count = render.grid_count
+    a.sub_steps = render.anti_aliasing
+    a.screen_transform = lens_mod.screen_transform(render.resolution, sensor_size)
+    a.intensity = float(np.float32(project.flare.light.intensity * 1e3))
+    a.ghost_scale = 1 - lens.fstop / 32
+    a.ghost_height, a.ghost_width = ghost_shape[0], ghost_shape[1]
+    if a.sub_steps not in (1, 2, 4, 8):
+        raise RealflareError('anti_aliasing must be 1, 2, 4 or 8')
+    return a
+
+
+def quad_constants(project: Project) -> tuple:
+    """(area_orig, rel_min_area) of ``rasterizing.py:328-329``."""
+    area = lens_mod.area_orig(project.render.grid_count, project.render.grid_length)
+    return area, project.flare.lens.min_area * area
