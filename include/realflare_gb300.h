@@ -86,6 +86,8 @@ typedef struct rf_raster_args {
 const char* rf_version(void);
 /* Text of the last CUDA error seen by this thread (empty if none). */
 const char* rf_last_cuda_error(void);
+/* Number of kernels this library has launched in this process (all threads). */
+long long rf_launch_count(void);
 
 /* ---- ray trace ---------------------------------------------------------------------- */
 /* Replaces RaytracingTask.raytrace's kernel launch (realflare/api/tasks/raytracing.py:
@@ -125,20 +127,30 @@ int rf_bin_masks(const float* bounds, int32_t prim_count, float screen_transform
                  int32_t width, int32_t height, int32_t bin_size, uint64_t* masks,
                  void* stream);
 
-/* Scratch bytes rf_bin_tiles needs for prim_count primitives, a pair capacity and the
- * tile grid of args (width, height, bin_size, tile_size). */
-int rf_bin_workspace_size(int32_t prim_count, int64_t pair_capacity, const rf_raster_args* args,
-                          size_t* bytes);
+/* Scratch bytes rf_bin_tiles needs for the render settings in args and an entry
+ * capacity (entries = (primitive, wavelength pair, tile) triples). */
+int rf_bin_workspace_size(const rf_raster_args* args, int64_t entry_capacity, size_t* bytes);
 
-/* Ordered per-tile primitive lists: for every raster tile, the indices of the primitives
- * whose reference bin (bin_size) contains the tile and whose conservative pixel bounds
- * touch it, in increasing primitive order. tile_offsets: device uint32[tiles + 1];
- * tile_prims: device uint32[pair_capacity]. The pair count is copied to the host
- * (one stream synchronisation); if it exceeds pair_capacity the call returns
- * RF_ERR_WORKSPACE and writes the count to *pair_count without filling the lists. */
-int rf_bin_tiles(const float* bounds, int32_t prim_count, const rf_raster_args* args,
+/* Ordered per-tile work lists for rf_raster. An entry is one (primitive, wavelength pair)
+ * of the reference's rasteriser loop (rasterizing.cl:573-653) on one raster tile. A tile
+ * receives the entry when the primitive's reference bin (bin_size, exactly the test of
+ * rasterizing.cl:449-453) contains the tile, and the conservative pixel bounds of the
+ * pair's quads touch the tile (pairs whose vertices lie beyond +-(2^14-1) samples, where
+ * the reference's 32-bit edge functions can wrap, go to every tile of the reference bin).
+ * Pairs with an invalid ray among their endpoint vertices contribute nothing and get no
+ * entry. Lists are in increasing (primitive, pair) order, the reference's per-pixel
+ * summation order. bounds: rf_quad_setup output; vertexes: rf_vertex output;
+ * tile_offsets: device uint32[tiles + 1]; tile_entries: device uint32[entry_capacity]
+ * holding primitive * max(W - 1, 1) + pair. The entry count is copied to the host (one
+ * stream synchronisation); if it exceeds entry_capacity the call returns RF_ERR_WORKSPACE
+ * with the count in *entry_count and leaves the lists unfilled. */
+int rf_bin_tiles(const float* bounds, const float* vertexes, const rf_raster_args* args,
                  void* workspace, size_t workspace_bytes, uint32_t* tile_offsets,
-                 uint32_t* tile_prims, int64_t pair_capacity, int64_t* pair_count, void* stream);
+                 uint32_t* tile_entries, int64_t entry_capacity, int64_t* entry_count,
+                 void* stream);
+
+/* Raster tile grid of args: writes the tile edge (resolving tile_size 0) and tile count. */
+int rf_raster_tiles(const rf_raster_args* args, int32_t* tile_size, int32_t* tile_count);
 
 /* ---- raster ------------------------------------------------------------------------- */
 /* Replaces the rasterizer kernel (realflare/api/tasks/cl/rasterizing.cl:524-663), its
@@ -146,7 +158,7 @@ int rf_bin_tiles(const float* bounds, int32_t prim_count, const rf_raster_args* 
  * 387-418) and fragment_shader / xyz_to_ap1 (rasterizing.cl:471-522, color.cl:3-10).
  * ghost: device float[ghost_height][ghost_width]; spectrum: device float[340][4] (CIE XYZ0
  * 390..729 nm); image: device float[height][width][4] RGBA (AP1, alpha 0, row 0 = top). */
-int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_prims,
+int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
               const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
               void* stream);
 

@@ -49,7 +49,7 @@ class Oracle:
             lib.rfo_vertex.argtypes = [_P, _P, _I, _I, _I, _F, _I, _I, _P]
             lib.rfo_bin_masks.argtypes = [_P, _I, _F, _I, _I, _I, _P]
             lib.rfo_raster.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P]
-            lib.rfo_raster_rows.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P, _I, _I]
+            lib.rfo_raster_rows.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P, _I, _I, _I, _I]
             lib.rfo_aperture_shape.argtypes = [_P, _I, _I, _F, _F, _I, _F, _F, _F]
             lib.rfo_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
             lib.rfo_aperture_noise_dust.argtypes = [_P, _P, _I, _I, _F, _F]
@@ -93,7 +93,7 @@ class Oracle:
         self.lib.rfo_bin_masks(_ptr(_c(bounds, np.float32)), prims, st, width, height, bin_size, _ptr(masks))
         return masks
 
-    def raster(self, vertexes, masks, ghost, spectrum, args: RasterArgs, rows=None):
+    def raster(self, vertexes, masks, ghost, spectrum, args: RasterArgs, rows=None, cols=(0, 0)):
         image = np.zeros((args.height, args.width, 4), np.float32)
         v = _c(vertexes, np.float32)
         m = _c(masks, np.uint64)
@@ -103,7 +103,7 @@ class Oracle:
             self.lib.rfo_raster(_ptr(v), _ptr(m), masks.shape[1], _ptr(g), _ptr(s), ctypes.byref(args), _ptr(image))
         else:
             self.lib.rfo_raster_rows(_ptr(v), _ptr(m), masks.shape[1], _ptr(g), _ptr(s), ctypes.byref(args),
-                                     _ptr(image), rows[0], rows[1])
+                                     _ptr(image), rows[0], rows[1], cols[0], cols[1])
         return image
 
     def aperture_shape(self, w, h, size, blades, rotation, roundness, softness):
@@ -156,7 +156,7 @@ class Reference:
             lib.ref_vertex_shader.argtypes = [_P, _P, _I, _I, _I, _F, _I, _I, _P]
             lib.ref_binner.argtypes = [_P, _I, _F, _I, _I, _I, _I, _P]
             lib.ref_rasterizer.argtypes = [_P, _P, _I, _P, _I, _I, _P, _I, _I, _I, _I, _I, _F, _F, _I, _I, _I,
-                                           _I, _I, _P]
+                                           _I, _I, _I, _I, _P]
             lib.ref_starburst.argtypes = [_P, _I, _I, _P, _I, _F, _F, _F, _P, _F, _P, _P, _I, _I, _I, _I, _P]
             lib.ref_aperture_shape.argtypes = [_P, _I, _I, _F, _F, _I, _F, _F, _F]
             lib.ref_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
@@ -200,7 +200,7 @@ class Reference:
                             _ptr(masks))
         return masks
 
-    def rasterizer(self, vertexes, masks, ghost, spectrum, args: RasterArgs, rows=None):
+    def rasterizer(self, vertexes, masks, ghost, spectrum, args: RasterArgs, rows=None, cols=(0, 0)):
         image = np.zeros((args.height, args.width, 4), np.float32)
         y0, y1 = rows if rows is not None else (0, args.height)
         g = _c(ghost, np.float32)
@@ -208,7 +208,7 @@ class Reference:
                                 _ptr(g), g.shape[1], g.shape[0], _ptr(_c(spectrum, np.float32)), args.path_count,
                                 args.wavelength_count, args.wavelength_sub_count, args.grid_count, args.sub_steps,
                                 args.intensity, args.ghost_scale, args.width, args.height, args.bin_size, y0, y1,
-                                _ptr(image))
+                                cols[0], cols[1], _ptr(image))
         return image
 
     def starburst(self, fourier, spectrum, a: StarburstArgs, rows=None):

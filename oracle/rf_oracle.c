@@ -704,15 +704,16 @@ int rfo_raster(const float* vertexes, const uint64_t* masks, int batch_count, co
     return 0;
 }
 
-/* Rasterise rows [y0, y1) only (CPU baseline samples). */
+/* Rasterise pixels [x0, x1) x [y0, y1) only (CPU baseline samples). */
 int rfo_raster_rows(const float* vertexes, const uint64_t* masks, int batch_count, const float* ghost,
-                    const float* spectrum, const rf_raster_args* a, float* image, int y0, int y1) {
+                    const float* spectrum, const rf_raster_args* a, float* image, int y0, int y1, int x0, int x1) {
     const int B = a->bin_size;
     const int bdx = (a->width + B - 1) / B;
     const long long prim_total = (long long)a->path_count * (a->grid_count - 1) * (a->grid_count - 1);
-#pragma omp parallel for schedule(dynamic, 1)
+    if (x1 <= 0 || x1 > a->width) x1 = a->width;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
     for (int y = y0; y < y1; y++) {
-        for (int x = 0; x < a->width; x++) {
+        for (int x = x0; x < x1; x++) {
             int bin = (y / B) * bdx + (x / B);
             real rgb[3] = {0, 0, 0};
             for (int batch = 0; batch < batch_count; batch++) {

@@ -95,9 +95,10 @@ SIGNATURES = {
     'rf_quad_setup': [P, I32, I32, I32, F32, F32, P, P, P],
     'rf_vertex': [P, P, I32, I32, I32, F32, I32, I32, P, P],
     'rf_bin_masks': [P, I32, F32, I32, I32, I32, P, P],
-    'rf_bin_workspace_size': [I32, I64, ctypes.POINTER(RasterArgs), ctypes.POINTER(ctypes.c_size_t)],
-    'rf_bin_tiles': [P, I32, ctypes.POINTER(RasterArgs), P, ctypes.c_size_t, P, P, I64,
+    'rf_bin_workspace_size': [ctypes.POINTER(RasterArgs), I64, ctypes.POINTER(ctypes.c_size_t)],
+    'rf_bin_tiles': [P, P, ctypes.POINTER(RasterArgs), P, ctypes.c_size_t, P, P, I64,
                      ctypes.POINTER(ctypes.c_int64), P],
+    'rf_raster_tiles': [ctypes.POINTER(RasterArgs), ctypes.POINTER(I32), ctypes.POINTER(I32)],
     'rf_raster': [P, P, P, P, P, ctypes.POINTER(RasterArgs), P, P],
     'rf_raster_masks': [P, P, I32, P, P, ctypes.POINTER(RasterArgs), P, P],
     'rf_fft2': [P, P, I32, I32, I32, I32, F32, P],
@@ -128,6 +129,7 @@ def lib() -> ctypes.CDLL:
             fn.restype = ctypes.c_int
         handle.rf_version.restype = ctypes.c_char_p
         handle.rf_last_cuda_error.restype = ctypes.c_char_p
+        handle.rf_launch_count.restype = ctypes.c_longlong
         _lib = handle
     return _lib
 

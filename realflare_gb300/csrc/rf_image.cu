@@ -1,0 +1,229 @@
+// rf_image.cu — per-pixel image kernels: the starburst compositor, the aperture masks and
+// the flare/starburst composite.
+//
+// k_starburst follows realflare/api/tasks/cl/starburst.cl:1-87 with noise.cl:1-5 and
+// geometry.cl:1-48; k_aperture_shape / k_aperture_dust follow aperture.cl:5-47 / 139-174.
+#include <math.h>
+
+#include <cmath>
+
+#include "rf_common.cuh"
+
+namespace rf {
+namespace {
+
+__device__ __forceinline__ float fract1(float x) { return fminf(x - floorf(x), 0x1.fffffep-1f); }
+// noise(x, y, z) of noise.cl:1-5
+__device__ __forceinline__ float noise3(float x, float y, float z) {
+    return fract1(sinf(x * 112.9898f + y * 179.233f + z * 237.212f) * 43758.5453f);
+}
+__device__ __forceinline__ void ndc_of(int px, int py, int w, int h, float& nx, float& ny) {
+    nx = 2.0f * ((float)px / (float)(w - 1)) - 1.0f;
+    ny = 2.0f * ((float)py / (float)(h - 1)) - 1.0f;
+}
+__device__ __forceinline__ void rot2(float& x, float& y, float angle) {
+    float s, c;
+    sincosf(angle, &s, &c);
+    const float nx = x * c + y * s, ny = y * c - x * s;
+    x = nx;
+    y = ny;
+}
+
+__global__ void __launch_bounds__(256) k_starburst(const float* __restrict__ spectrum,
+                                                   const float* __restrict__ light, rf_starburst_args a,
+                                                   float4* __restrict__ image) {
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= a.width || y >= a.height) return;
+    float nx, ny;
+    ndc_of(x, y, a.width, a.height, nx, ny);
+    nx = (nx - a.offset[0]) / fmaxf(a.scale[0], 1.17549435e-38f);
+    ny = (ny - a.offset[1]) / fmaxf(a.scale[1], 1.17549435e-38f);
+    const size_t plane = (size_t)a.spectrum_width * a.spectrum_height;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const float fx = (float)x, fy = (float)y;
+    for (int t = 0; t < a.samples; t++) {
+        const float step = (float)t / (float)a.samples;
+        const float wavelength = step * (float)(RF_LAMBDA_MAX - RF_LAMBDA_MIN) + (float)RF_LAMBDA_MIN;
+        const float seed = (float)(t * 4);
+        float px = nx, py = ny;
+        const float radius = a.blur * sqrtf(noise3(fx, fy, seed));
+        const float alpha = noise3(fx, fy, seed + 1.0f) * 2.0f * RF_MPI_F;
+        float sa, ca;
+        sincosf(alpha, &sa, &ca);
+        px += ca * radius;
+        py += sa * radius;
+        // chromatic scale 1 - (1 - lambda / 560) (LAMBDA_MID is an int in starburst.cl)
+        const float sc = fmaxf(1.0f - (1.0f - (wavelength / (float)RF_LAMBDA_MID)) * 1.0f, 1.17549435e-38f);
+        px = px / sc;
+        py = py / sc;
+        const float sign = noise3(fx, fy, seed + 2.0f) > 0.5f ? 1.0f : -1.0f;
+        const float angle = sign * a.rotation * (1.0f - powf(noise3(fx, fy, seed + 3.0f), a.rotation_weight));
+        rot2(px, py, angle);
+        const float u = px * 0.5f + 0.5f, v = py * 0.5f + 0.5f;
+        int sidx = 0;
+        if (a.spectrum_count > 1) {
+            const int k = cvt_rz_sat(floorf((wavelength - a.lambda_first) / a.lambda_step + 0.5f));
+            sidx = k < 0 ? 0 : (k >= a.spectrum_count ? a.spectrum_count - 1 : k);
+        }
+        const float fi = sample_linear(spectrum + sidx * plane, a.spectrum_width, a.spectrum_height, 1, 0, u, v, false);
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[c] += sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, c, step, 0.0f, false) * fi;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[c] = acc[c] / (float)a.samples;
+    if (!isnan(a.vignetting[0])) {
+        const float sdf = sqrtf(nx * nx + ny * ny) - 0.0f;
+        const float f = smoothstepf(a.vignetting[1], a.vignetting[0], sdf);
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[c] *= f;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[c] *= a.intensity;
+    image[(size_t)y * a.width + x] = xyz_to_ap1(acc[0], acc[1], acc[2]);
+}
+
+__global__ void __launch_bounds__(256) k_aperture_shape(float* __restrict__ image, int w, int h, float sx, float sy,
+                                                        int blades, float rotation, float roundness, float softness) {
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= w || y >= h) return;
+    float px, py;
+    ndc_of(x, y, w, h, px, py);
+    px = px / fmaxf(sx, 1.17549435e-38f);
+    py = py / fmaxf(sy, 1.17549435e-38f);
+    rot2(px, py, rotation);
+    float sdf = 0.0f;
+    for (int i = 0; i < blades; i++) {
+        const float angle = ((float)i / (float)blades + 0.25f) * 2.0f * RF_MPI_F;
+        float s, c;
+        sincosf(angle, &s, &c);
+        sdf = fmaxf(sdf, c * px + s * py);
+    }
+    const float cg = atan2f(-px, -py) / (2.0f * RF_MPI_F) + 0.5f;
+    const float bg = fmodf(cg * (float)blades + 0.5f, 1.0f);
+    sdf += sinf(bg * RF_MPI_F) * roundness;
+    image[(size_t)y * w + x] = 1.0f - smoothstepf(1.0f - softness, 1.0f + softness, sdf);
+}
+
+__global__ void __launch_bounds__(256) k_aperture_dust(float* __restrict__ image, int w, int h, float sx, float sy,
+                                                       float strength, int count, float radius, float par_x,
+                                                       float par_y, float softness) {
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= w || y >= h) return;
+    float px, py;
+    ndc_of(x, y, w, h, px, py);
+    px = px / fmaxf(sx, 1.17549435e-38f);
+    py = py / fmaxf(sy, 1.17549435e-38f);
+    float sdf = 1.0f;
+    for (int i = 0; i < count; i++) {
+        float cx = noise3((float)i, (float)count, 0.0f) + par_x;
+        float cy = noise3((float)i, (float)count, 1.0f) + par_y;
+        cx = fmodf(1.0f + fmodf(cx, 1.0f), 1.0f) * 2.0f - 1.0f;
+        cy = fmodf(1.0f + fmodf(cy, 1.0f), 1.0f) * 2.0f - 1.0f;
+        const float dx = px - cx, dy = py - cy;
+        sdf = fminf(sdf, sqrtf(dx * dx + dy * dy) - radius);
+    }
+    float v = image[(size_t)y * w + x];
+    v *= 1.0f - (strength * smoothstepf(softness, -softness, sdf));
+    image[(size_t)y * w + x] = v;
+}
+
+// Separable Gaussian over the noise (no reference counterpart): pass 0 blurs rows into
+// tmp, pass 1 blurs columns of tmp and multiplies the image by 1 - strength * blur.
+struct BlurWeights {
+    float w[513];
+    int rad;
+};
+
+__global__ void __launch_bounds__(256) k_noise_blur(const float* __restrict__ src, float* __restrict__ dst,
+                                                    float* __restrict__ image, int w, int h,
+                                                    const __grid_constant__ BlurWeights bw, int pass, float strength) {
+    const int rad = bw.rad;
+    const float* weights = bw.w;
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= w || y >= h) return;
+    float acc = 0.0f;
+    for (int k = -rad; k <= rad; k++) {
+        int xx = x, yy = y;
+        if (pass == 0) xx = min(max(x + k, 0), w - 1);
+        else yy = min(max(y + k, 0), h - 1);
+        acc += weights[k + rad] * src[(size_t)yy * w + xx];
+    }
+    if (pass == 0) dst[(size_t)y * w + x] = acc;
+    else image[(size_t)y * w + x] = image[(size_t)y * w + x] * (1.0f - strength * acc);
+}
+
+__global__ void k_axpby(const float* __restrict__ a, float wa, const float* __restrict__ b, float wb,
+                        float* __restrict__ out, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] * wa + b[i] * wb;
+}
+
+}  // namespace
+}  // namespace rf
+
+extern "C" int rf_starburst(const float* spectrum, const float* light_spectrum, const rf_starburst_args* args,
+                            float* image, void* stream) {
+    using namespace rf;
+    if (!spectrum || !light_spectrum || !args || !image) return RF_ERR_INVALID_ARG;
+    const rf_starburst_args& a = *args;
+    if (a.width < 2 || a.height < 2 || a.samples < 1 || a.spectrum_width < 1 || a.spectrum_height < 1 ||
+        a.spectrum_count < 1 || !aligned16(image))
+        return RF_ERR_INVALID_ARG;
+    dim3 grid((a.width + 15) / 16, (a.height + 15) / 16);
+    k_starburst<<<grid, 256, 0, (cudaStream_t)stream>>>(spectrum, light_spectrum, a, (float4*)image);
+    return launch_status();
+}
+
+extern "C" int rf_aperture_shape(float* image, int32_t width, int32_t height, float size_x, float size_y,
+                                 int32_t blades, float rotation, float roundness, float softness, void* stream) {
+    using namespace rf;
+    if (!image || width < 2 || height < 2 || blades < 0) return RF_ERR_INVALID_ARG;
+    dim3 grid((width + 15) / 16, (height + 15) / 16);
+    k_aperture_shape<<<grid, 256, 0, (cudaStream_t)stream>>>(image, width, height, size_x, size_y, blades, rotation,
+                                                             roundness, softness);
+    return launch_status();
+}
+
+extern "C" int rf_aperture_dust(float* image, int32_t width, int32_t height, float size_x, float size_y,
+                                float strength, float density, float radius, float parallax_x, float parallax_y,
+                                float softness, void* stream) {
+    using namespace rf;
+    if (!image || width < 2 || height < 2) return RF_ERR_INVALID_ARG;
+    // int count = fmin(density, 1) * 1000 (aperture.cl:160)
+    const int count = (int)(fminf(density, 1.0f) * 1000.0f);
+    dim3 grid((width + 15) / 16, (height + 15) / 16);
+    k_aperture_dust<<<grid, 256, 0, (cudaStream_t)stream>>>(image, width, height, size_x, size_y, strength, count,
+                                                            radius, parallax_x, parallax_y, softness);
+    return launch_status();
+}
+
+extern "C" int rf_aperture_noise_dust(float* image, const float* noise, float* scratch, int32_t width,
+                                      int32_t height, float strength, float sigma, void* stream) {
+    using namespace rf;
+    if (!image || !noise || !scratch || width < 1 || height < 1 || !(sigma >= 0.0f) || sigma > 64.0f)
+        return RF_ERR_INVALID_ARG;
+    // weights exp(-k^2 / (2 sigma^2)) normalised to 1 in FP32 (the oracle's values),
+    // passed by value
+    BlurWeights bw;
+    bw.rad = (int)std::ceil((double)sigma * 4.0);
+    float sum = 0.0f;
+    for (int k = -bw.rad; k <= bw.rad; k++) {
+        bw.w[k + bw.rad] = sigma > 0.0f ? expf(-(float)(k * k) / (2.0f * sigma * sigma)) : 1.0f;
+        sum += bw.w[k + bw.rad];
+    }
+    for (int k = 0; k <= 2 * bw.rad; k++) bw.w[k] = bw.w[k] / sum;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 grid((width + 15) / 16, (height + 15) / 16);
+    k_noise_blur<<<grid, 256, 0, s>>>(noise, scratch, image, width, height, bw, 0, strength);
+    RF_TRY(launch_status());
+    k_noise_blur<<<grid, 256, 0, s>>>(scratch, nullptr, image, width, height, bw, 1, strength);
+    return launch_status();
+}
+
+extern "C" int rf_axpby(const float* a, float wa, const float* b, float wb, float* out, int64_t n, void* stream) {
+    using namespace rf;
+    if (!a || !b || !out || n < 0) return RF_ERR_INVALID_ARG;
+    if (n == 0) return RF_OK;
+    k_axpby<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a, wa, b, wb, out, n);
+    return launch_status();
+}

@@ -1,0 +1,172 @@
+// rf_quad.cu — quad setup (prim_shader) and vertex setup (vertex_shader).
+//
+// Both follow realflare/api/tasks/cl/rasterizing.cl (prim_shader 233-320, vertex_shader
+// 322-386, quad_vertexes 218-230, quad_neighbors 196-216). This file is compiled without
+// fused multiply-add contraction, so for identical rays the bounds, intensities and
+// vertex positions equal the oracle's bit for bit. Both kernels are memory-bound: one
+// thread per primitive (reading its 4 corner rays per wavelength) and one thread per ray
+// (coalesced plane reads, one 32-byte vertex store).
+#include "rf_common.cuh"
+
+namespace rf {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float edge_f(float ax, float ay, float bx, float by, float cx, float cy) {
+    return (ax - bx) * (cy - ay) - (ay - by) * (cx - ax);
+}
+
+__global__ void __launch_bounds__(kThreads) k_quad_setup(const float* __restrict__ rays, int P, int W, int G,
+                                                         long long n_rays, float area_orig, float min_area,
+                                                         float4* __restrict__ bounds, float* __restrict__ inten) {
+    const int Q = (G - 1) * (G - 1), R = G * G;
+    const long long pq = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (pq >= (long long)P * Q) return;
+    const int path = (int)(pq / Q), quad = (int)(pq % Q);
+    const int row = quad / (G - 1), col = quad % (G - 1);
+    int v[4];
+    v[0] = row * G + col;
+    v[1] = v[0] + 1;
+    v[2] = v[1] + G;
+    v[3] = v[0] + G;
+    const float* pos_x = rays;
+    const float* pos_y = rays + n_rays;
+    const float* rrel = rays + 4 * n_rays;
+    const float* refl = rays + 5 * n_rays;
+    float bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY;
+    int invalid_rrel = 0;
+    bool culled = false;
+    for (int w = 0; w < W; w++) {
+        const size_t prim_index = (size_t)pq * W + w;
+        if (culled) {
+            inten[prim_index] = 0.0f;  // the reference leaves these entries stale
+            continue;
+        }
+        const size_t off = ((size_t)path * W + w) * R;
+        float px[4], py[4], rr[4];
+        int valid = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            rr[i] = __ldg(rrel + off + v[i]);
+            float x = __ldg(pos_x + off + v[i]), y = __ldg(pos_y + off + v[i]);
+            if (!isnan(__ldg(refl + off + v[i]))) {
+                // compaction into the first free slot (valid <= i)
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (k == valid) {
+                        px[k] = x;
+                        py[k] = y;
+                    }
+                valid++;
+            }
+        }
+        float area;
+        if (valid == 4) {
+            float a0 = edge_f(px[0], py[0], px[1], py[1], px[2], py[2]);
+            float a1 = edge_f(px[0], py[0], px[2], py[2], px[3], py[3]);
+            area = fabsf(a0 + a1) / 2.0f;
+        } else if (valid == 3) {
+            area = fabsf(edge_f(px[0], py[0], px[1], py[1], px[2], py[2]));
+            px[3] = px[2];
+            py[3] = py[2];
+            rr[3] = rr[2];
+        } else {
+            culled = true;
+            inten[prim_index] = 0.0f;
+            continue;
+        }
+        if (rr[0] > 1.0f && rr[1] > 1.0f && rr[2] > 1.0f && rr[3] > 1.0f) invalid_rrel++;
+        float area_actual = fmaxf(area, min_area);
+        inten[prim_index] = area_actual > 0.0f ? area_orig / area_actual : 0.0f;
+        bx0 = fminf(bx0, fminf(fminf(px[0], px[1]), fminf(px[2], px[3])));
+        by0 = fminf(by0, fminf(fminf(py[0], py[1]), fminf(py[2], py[3])));
+        bx1 = fmaxf(bx1, fmaxf(fmaxf(px[0], px[1]), fmaxf(px[2], px[3])));
+        by1 = fmaxf(by1, fmaxf(fmaxf(py[0], py[1]), fmaxf(py[2], py[3])));
+    }
+    if (invalid_rrel == W) culled = true;
+    bounds[pq] = make_float4(culled ? __int_as_float(0x7fffffff) : bx0, by0, bx1, by1);
+}
+
+__global__ void __launch_bounds__(kThreads) k_vertex(const float* __restrict__ rays, const float* __restrict__ inten,
+                                                     int P, int W, int G, long long n_rays, float st, float half_w,
+                                                     float half_h, float4* __restrict__ vertexes) {
+    const int Q = (G - 1) * (G - 1), R = G * G;
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;  // ray-plane order
+    if (i > n_rays) return;
+    if (i == n_rays) {  // the zero vertex after the last one
+        vertexes[2 * n_rays] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vertexes[2 * n_rays + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const int ray_id = (int)(i % R);
+    const long long pw = i / R;
+    const int w = (int)(pw % W);
+    const int path = (int)(pw / W);
+    const long long vi = ((long long)path * R + ray_id) * W + w;  // the reference's order
+    const float refl = __ldg(rays + 5 * n_rays + i);
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, refl, 0.f, 0.f);
+    if (!isnan(refl)) {
+        const int x = ray_id % G, y = ray_id / G;
+        int nb[4];
+        nb[0] = (y - 1) * (G - 1) + (x - 1);
+        nb[1] = nb[0] + 1;
+        nb[2] = y * (G - 1) + (x - 1);
+        nb[3] = nb[2] + 1;
+        float s = 0.0f;
+        int count = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (nb[k] < 0 || nb[k] >= Q) continue;
+            float v = __ldg(inten + ((size_t)path * Q + nb[k]) * W + w);
+            if (v > 0.0f) {
+                s += v;
+                ++count;
+            }
+        }
+        s /= (float)(count > 1 ? count : 1);
+        a.x = __fadd_rn(__fmul_rn(__ldg(rays + i), st), half_w);
+        a.y = __fadd_rn(__fmul_rn(__ldg(rays + n_rays + i), st), half_h);
+        a.z = __ldg(rays + 2 * n_rays + i);
+        a.w = __ldg(rays + 3 * n_rays + i);
+        b.x = __ldg(rays + 4 * n_rays + i);
+        b.z = s;
+    }
+    vertexes[2 * vi] = a;
+    vertexes[2 * vi + 1] = b;
+}
+
+}  // namespace
+}  // namespace rf
+
+extern "C" int rf_quad_setup(const float* rays, int32_t path_count, int32_t wavelength_count, int32_t grid_count,
+                             float area_orig, float min_area, float* bounds, float* intensities, void* stream) {
+    using namespace rf;
+    if (!rays || !bounds || !intensities || path_count < 0 || wavelength_count < 1 || grid_count < 2)
+        return RF_ERR_INVALID_ARG;
+    if (!aligned16(bounds)) return RF_ERR_INVALID_ARG;
+    const long long Q = (long long)(grid_count - 1) * (grid_count - 1);
+    const long long n = (long long)path_count * Q;
+    if (n == 0) return RF_OK;
+    const long long n_rays = (long long)path_count * wavelength_count * grid_count * grid_count;
+    k_quad_setup<<<blocks_for(n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        rays, path_count, wavelength_count, grid_count, n_rays, area_orig, min_area, (float4*)bounds, intensities);
+    return launch_status();
+}
+
+extern "C" int rf_vertex(const float* rays, const float* intensities, int32_t path_count, int32_t wavelength_count,
+                         int32_t grid_count, float screen_transform, int32_t width, int32_t height, float* vertexes,
+                         void* stream) {
+    using namespace rf;
+    if (!rays || !intensities || !vertexes || path_count < 0 || wavelength_count < 1 || grid_count < 2 ||
+        width < 1 || height < 1)
+        return RF_ERR_INVALID_ARG;
+    if (!aligned16(vertexes)) return RF_ERR_INVALID_ARG;
+    const long long n_rays = (long long)path_count * wavelength_count * grid_count * grid_count;
+    // convert_float2(resolution) / 2 (rasterizing.cl:374)
+    const float half_w = (float)width / 2.0f, half_h = (float)height / 2.0f;
+    k_vertex<<<blocks_for(n_rays + 1, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        rays, intensities, path_count, wavelength_count, grid_count, n_rays, screen_transform, half_w, half_h,
+        (float4*)vertexes);
+    return launch_status();
+}

@@ -1,0 +1,613 @@
+// rf_raster.cu — the ghost rasteriser.
+//
+// Per pixel the result is the reference's (realflare/api/tasks/cl/rasterizing.cl:524-663):
+// the sum over visible primitives (in primitive order), wavelength pairs and sub-wavelength
+// steps of XYZ(lambda) * fragment, where a fragment is the n-rook sample coverage of the
+// integer quad (intersect_quad 55-93) times the mean-value interpolated ghost texture,
+// housing falloff, area intensity and coating reflectance (compute_barycentric_quad
+// 95-148, fragment_shader 471-506, mix_vertex 509-522), scaled and converted to AP1
+// (color.cl:3-10) and written y-flipped.
+//
+// GB300 organisation (k_raster): one CTA per T x T tile, threads own pixels (T = 32: 256
+// threads x 4 pixels). The tile's list from rf_bin_tiles holds (primitive, wavelength pair)
+// entries in increasing order. Entries are expanded in batches into shared-memory records
+// (one per sub-wavelength step): the mixed integer vertices, the five edge functions as
+// wrapping-int32 plane coefficients with the top-left bias folded in, the integer bounds
+// and the mixed attributes, set up once by one thread each. Every pixel then walks the
+// records in order, so its sum runs in the reference's order; a pixel whose samples lie
+// outside a record's integer bounds skips it (exact: with vertex and sample coordinates
+// below 2^14 the edge functions cannot wrap, and the quad test then never accepts a
+// sample outside the bounds; records beyond that range are tested at every pixel).
+//
+// k_raster_masks is the literal per-pixel loop over the reference's bin masks, used for
+// parity checks of the binner and the rasteriser.
+#include <stddef.h>
+
+#include "rf_common.cuh"
+
+namespace rf {
+int tile_size_of(const rf_raster_args& a);
+
+namespace {
+
+constexpr int kBatchRecords = 128;
+
+struct alignas(16) Rec {
+    int bb[4];       // xmin, xmax, ymin, ymax (first: read as one 16-byte vector)
+    int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
+    int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
+    int flags;       // 1: bounds rejection is exact; 2: both triangles collinear (never inside)
+    int color;       // w * WS + i
+    float uv[8], rrel[4], inten[4], refl[4];
+};
+static_assert(sizeof(Rec) % 16 == 0 && offsetof(Rec, bb) == 0, "records are read with 16-byte loads");
+
+struct RasterParams {
+    int width, height, T, ntx, S, W, WS, G, maxW;
+    float intensity, ghost_scale;
+    int ghost_w, ghost_h;
+    bool safe_screen;
+};
+
+__device__ __forceinline__ bool top_left(int ax, int ay, int bx, int by) {
+    int ex = wsub(bx, ax), ey = wsub(by, ay);
+    return (ey == 0 && ex > 0) || ey > 0;
+}
+
+__device__ __forceinline__ int32_t edge_i(int ax, int ay, int bx, int by, int cx, int cy) {
+    return wsub(wmul(wsub(ax, bx), wsub(cy, ay)), wmul(wsub(ay, by), wsub(cx, ax)));
+}
+
+__device__ __forceinline__ void edge_coeffs(int ax, int ay, int bx, int by, int* e) {
+    // (a.x - b.x) * (p.y - a.y) - (a.y - b.y) * (p.x - a.x) + bias, as A*p.y + B*p.x + C
+    const int A = wsub(ax, bx);
+    const int dy = wsub(ay, by);
+    e[0] = A;
+    e[1] = wsub(0, dy);
+    e[2] = wadd(wsub(wmul(dy, ax), wmul(A, ay)), top_left(ax, ay, bx, by) ? 0 : -1);
+}
+
+// intersect_quad (rasterizing.cl:55-93) from plane coefficients
+__device__ __forceinline__ bool inside(const Rec& r, int px, int py) {
+    const int* e = r.ec;
+    const bool w01 = wadd(wadd(wmul(e[0], py), wmul(e[1], px)), e[2]) >= 0;
+    const bool w12 = wadd(wadd(wmul(e[3], py), wmul(e[4], px)), e[5]) >= 0;
+    const bool w23 = wadd(wadd(wmul(e[6], py), wmul(e[7], px)), e[8]) >= 0;
+    const bool w30 = wadd(wadd(wmul(e[9], py), wmul(e[10], px)), e[11]) >= 0;
+    const bool w20 = wadd(wadd(wmul(e[12], py), wmul(e[13], px)), e[14]) >= 0;
+    const bool front = (w20 && w01 && w12 && (w23 || w30)) || (!w20 && w23 && w30 && (w01 || w12));
+    const bool back = (!w20 && !w01 && !w12 && (!w23 || !w30)) || (w20 && !w23 && !w30 && (!w01 || !w12));
+    return front || back;
+}
+
+// compute_barycentric_quad (rasterizing.cl:95-148)
+__device__ __forceinline__ void barycentric(const int* q, int px, int py, float w[4]) {
+    float sx[4], sy[4], a[4], d[4], r[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        sx[i] = (float)wsub(q[2 * i], px);
+        sy[i] = (float)wsub(q[2 * i + 1], py);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = (i + 1) & 3;
+        a[i] = sx[i] * sy[j] - sx[j] * sy[i];
+        d[i] = sx[i] * sx[j] + sy[i] * sy[j];
+        r[i] = sqrtf(sx[i] * sx[i] + sy[i] * sy[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (r[i] == 0.0f) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) w[k] = (k == i) ? 1.0f : 0.0f;
+            return;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (a[i] == 0.0f) a[i] = 1e-3f;
+    float t[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) t[i] = (r[i] * r[(i + 1) & 3] - d[i]) / a[i];
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) / r[i];
+    const float sum = w[0] + w[1] + w[2] + w[3];
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = w[i] / sum;
+}
+
+// fragment_shader (rasterizing.cl:471-506) times the hit count
+__device__ __forceinline__ float fragment(const Rec& r, const float w[4], const float* __restrict__ ghost,
+                                          const RasterParams& p, int hits) {
+    float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
+    float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
+    u = (u / p.ghost_scale + 1.0f) / 2.0f;
+    v = (v / p.ghost_scale + 1.0f) / 2.0f;
+    const float gi = sample_linear(ghost, p.ghost_w, p.ghost_h, 1, 0, u, v, false);
+    const float rr = w[0] * r.rrel[0] + w[1] * r.rrel[1] + w[2] * r.rrel[2] + w[3] * r.rrel[3];
+    const float ri = smoothstepf(1.0f, 0.95f, rr);
+    float ai = w[0] * r.inten[0] + w[1] * r.inten[1] + w[2] * r.inten[2] + w[3] * r.inten[3];
+    float ci = w[0] * r.refl[0] + w[1] * r.refl[1] + w[2] * r.refl[2] + w[3] * r.refl[3];
+    ai = fmaxf(ai, 0.0f);
+    ci = fmaxf(ci, 0.0f);
+    return gi * ri * ai * ci * (float)hits;
+}
+
+// Expand entry (primitive, pair w) at sub step i into a record.
+__device__ void setup_record(const float4* __restrict__ vtx, uint32_t entry, int i, const float* blend,
+                             const RasterParams& p, Rec& r) {
+    const long long prim = entry / p.maxW;
+    const int w = (int)(entry % p.maxW);
+    const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
+    const long long path = prim / Q;
+    const int quad = (int)(prim % Q);
+    const int row = quad / (p.G - 1), col = quad % (p.G - 1);
+    const int c0 = row * p.G + col;
+    const int corners[4] = {c0, c0 + 1, c0 + 1 + p.G, c0 + p.G};
+    const float t = blend[i];
+    const float S = (float)p.S;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const long long vi = (path * VC + corners[k]) * p.W + w;
+        const float4 a0 = __ldg(vtx + 2 * vi), a1 = __ldg(vtx + 2 * vi + 1);
+        const float4 b0 = __ldg(vtx + 2 * vi + 2), b1 = __ldg(vtx + 2 * vi + 3);
+        // mix_vertex: x + (y - x) * t
+        const float px = a0.x + (b0.x - a0.x) * t, py = a0.y + (b0.y - a0.y) * t;
+        r.uv[2 * k] = a0.z + (b0.z - a0.z) * t;
+        r.uv[2 * k + 1] = a0.w + (b0.w - a0.w) * t;
+        r.rrel[k] = a1.x + (b1.x - a1.x) * t;
+        r.refl[k] = a1.y + (b1.y - a1.y) * t;
+        r.inten[k] = a1.z + (b1.z - a1.z) * t;
+        const float sx = px * S, sy = py * S;
+        finite = finite && fabsf(sx) < 16383.0f && fabsf(sy) < 16383.0f;
+        r.q[2 * k] = cvt_rz_sat(sx);
+        r.q[2 * k + 1] = cvt_rz_sat(sy);
+    }
+    const int* q = r.q;
+    edge_coeffs(q[0], q[1], q[2], q[3], r.ec + 0);
+    edge_coeffs(q[2], q[3], q[4], q[5], r.ec + 3);
+    edge_coeffs(q[4], q[5], q[6], q[7], r.ec + 6);
+    edge_coeffs(q[6], q[7], q[0], q[1], r.ec + 9);
+    edge_coeffs(q[4], q[5], q[0], q[1], r.ec + 12);
+    r.bb[0] = min(min(q[0], q[2]), min(q[4], q[6]));
+    r.bb[1] = max(max(q[0], q[2]), max(q[4], q[6]));
+    r.bb[2] = min(min(q[1], q[3]), min(q[5], q[7]));
+    r.bb[3] = max(max(q[1], q[3]), max(q[5], q[7]));
+    int flags = (finite && p.safe_screen) ? 1 : 0;
+    if (edge_i(q[0], q[1], q[2], q[3], q[4], q[5]) == 0 && edge_i(q[0], q[1], q[4], q[5], q[6], q[7]) == 0)
+        flags |= 2;
+    r.flags = flags;
+    r.color = w * p.WS + i;
+}
+
+// Mean-value weights (compute_barycentric_quad, rasterizing.cl:95-148). The half-angle
+// tangents t_i = (r_i r_j - d_i) / a_i amplify rounding where a_i is small next to
+// r_i r_j (and where a_i is 0 the reference divides the rounding residue of r_i r_j - d_i
+// by 1e-3): there t_i is evaluated with the reference's exact FP32 operations (correctly
+// rounded square roots, products, difference and quotient, never fused). Everywhere else,
+// and for the well-conditioned divisions by r_i and by the weight sum, reciprocal and
+// reciprocal-square-root instructions give the same values within a few ulps.
+__device__ __forceinline__ void barycentric_fast(const int* q, int px, int py, float w[4]) {
+    float sx[4], sy[4], a[4], d[4], r2[4], r[4], ir[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        sx[i] = (float)wsub(q[2 * i], px);
+        sy[i] = (float)wsub(q[2 * i + 1], py);
+    }
+    bool zero = false;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = (i + 1) & 3;
+        a[i] = __fsub_rn(__fmul_rn(sx[i], sy[j]), __fmul_rn(sx[j], sy[i]));
+        d[i] = __fadd_rn(__fmul_rn(sx[i], sx[j]), __fmul_rn(sy[i], sy[j]));
+        r2[i] = __fadd_rn(__fmul_rn(sx[i], sx[i]), __fmul_rn(sy[i], sy[i]));
+        zero = zero || r2[i] == 0.0f;
+        ir[i] = rsqrtf(r2[i]);
+        r[i] = r2[i] * ir[i];
+    }
+    if (zero) {  // a vertex on the sample point: one-hot on the first such vertex
+        int k = 0;
+#pragma unroll
+        for (int i = 3; i >= 0; i--)
+            if (sx[i] == 0.0f && sy[i] == 0.0f) k = i;
+#pragma unroll
+        for (int i = 0; i < 4; i++) w[i] = i == k ? 1.0f : 0.0f;
+        return;
+    }
+    float t[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = (i + 1) & 3;
+        if (a[i] * a[i] < (1.0f / 4096.0f) * r2[i] * r2[j]) {
+            const float ai = a[i] == 0.0f ? 1e-3f : a[i];
+            t[i] = __fdiv_rn(__fsub_rn(__fmul_rn(__fsqrt_rn(r2[i]), __fsqrt_rn(r2[j])), d[i]), ai);
+        } else {
+            t[i] = (r[i] * r[j] - d[i]) * __fdividef(1.0f, a[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) * ir[i];
+    const float inv = __fdividef(1.0f, w[0] + w[1] + w[2] + w[3]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] *= inv;
+}
+
+// fragment_shader (rasterizing.cl:471-506) times the hit count; inv_scale = 1 / ghost_scale
+__device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], const float* __restrict__ ghost,
+                                               const RasterParams& p, float inv_scale, int hits) {
+    float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
+    float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
+    u = (u * inv_scale + 1.0f) * 0.5f;
+    v = (v * inv_scale + 1.0f) * 0.5f;
+    const float gi = sample_linear(ghost, p.ghost_w, p.ghost_h, 1, 0, u, v, false);
+    const float rr = w[0] * r.rrel[0] + w[1] * r.rrel[1] + w[2] * r.rrel[2] + w[3] * r.rrel[3];
+    const float ri = smoothstepf(1.0f, 0.95f, rr);
+    float ai = w[0] * r.inten[0] + w[1] * r.inten[1] + w[2] * r.inten[2] + w[3] * r.inten[3];
+    float ci = w[0] * r.refl[0] + w[1] * r.refl[1] + w[2] * r.refl[2] + w[3] * r.refl[3];
+    ai = fmaxf(ai, 0.0f);
+    ci = fmaxf(ci, 0.0f);
+    return gi * ri * ai * ci * (float)hits;
+}
+
+// Corner k of entry `entry` at the pair's two wavelengths: vertex words a0, a1 (first
+// wavelength) and b0, b1 (second).
+struct CornerLoad {
+    float4 a0, a1, b0, b1;
+};
+__device__ __forceinline__ void load_corner(const float4* __restrict__ vtx, uint32_t entry, int k,
+                                            const RasterParams& p, CornerLoad& c) {
+    const long long prim = entry / p.maxW;
+    const int w = (int)(entry % p.maxW);
+    const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
+    const long long path = prim / Q;
+    const int quad = (int)(prim % Q);
+    const int c0 = (quad / (p.G - 1)) * p.G + quad % (p.G - 1);
+    const int corner = k == 0 ? c0 : (k == 1 ? c0 + 1 : (k == 2 ? c0 + 1 + p.G : c0 + p.G));
+    const long long vi = (path * VC + corner) * p.W + w;
+    c.a0 = __ldg(vtx + 2 * vi);
+    c.a1 = __ldg(vtx + 2 * vi + 1);
+    c.b0 = __ldg(vtx + 2 * vi + 2);
+    c.b1 = __ldg(vtx + 2 * vi + 3);
+}
+// mix_vertex (rasterizing.cl:509-522) of one corner into record r
+__device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t, int S, Rec& r) {
+    const float px = c.a0.x + (c.b0.x - c.a0.x) * t, py = c.a0.y + (c.b0.y - c.a0.y) * t;
+    r.uv[2 * k] = c.a0.z + (c.b0.z - c.a0.z) * t;
+    r.uv[2 * k + 1] = c.a0.w + (c.b0.w - c.a0.w) * t;
+    r.rrel[k] = c.a1.x + (c.b1.x - c.a1.x) * t;
+    r.refl[k] = c.a1.y + (c.b1.y - c.a1.y) * t;
+    r.inten[k] = c.a1.z + (c.b1.z - c.a1.z) * t;
+    r.q[2 * k] = cvt_rz_sat(px * (float)S);
+    r.q[2 * k + 1] = cvt_rz_sat(py * (float)S);
+}
+// edges, bounds and flags of a record whose corners are stored
+__device__ __forceinline__ void finish_record(const RasterParams& p, int w, int i, Rec& r) {
+    const int* q = r.q;
+    edge_coeffs(q[0], q[1], q[2], q[3], r.ec + 0);
+    edge_coeffs(q[2], q[3], q[4], q[5], r.ec + 3);
+    edge_coeffs(q[4], q[5], q[6], q[7], r.ec + 6);
+    edge_coeffs(q[6], q[7], q[0], q[1], r.ec + 9);
+    edge_coeffs(q[4], q[5], q[0], q[1], r.ec + 12);
+    r.bb[0] = min(min(q[0], q[2]), min(q[4], q[6]));
+    r.bb[1] = max(max(q[0], q[2]), max(q[4], q[6]));
+    r.bb[2] = min(min(q[1], q[3]), min(q[5], q[7]));
+    r.bb[3] = max(max(q[1], q[3]), max(q[5], q[7]));
+    // bounds rejection is exact while every coordinate stays below 2^14 - 1 in magnitude
+    const int lim = 16382;
+    bool safe = p.safe_screen;
+#pragma unroll
+    for (int k = 0; k < 8; k++) safe = safe && q[k] <= lim && q[k] >= -lim;
+    int flags = safe ? 1 : 0;
+    if (edge_i(q[0], q[1], q[2], q[3], q[4], q[5]) == 0 && edge_i(q[0], q[1], q[4], q[5], q[6], q[7]) == 0)
+        flags |= 2;
+    r.flags = flags;
+    r.color = w * p.WS + i;
+}
+
+// One CTA per 32 x 32 tile, 8 warps; warp w shades the four 8 x 4 pixel blocks
+// w, w + 8, w + 16, w + 24 (block b at column b % 4, row b / 4), so a record outside a
+// block's sample bounds is skipped by the whole warp at once.
+constexpr int kTile = 32;
+constexpr int kThreads = 256;
+
+__global__ void __launch_bounds__(kThreads, 3) k_raster(const float4* __restrict__ vtx,
+                                                       const uint32_t* __restrict__ tile_offsets,
+                                                       const uint32_t* __restrict__ tile_entries,
+                                                       const float* __restrict__ ghost,
+                                                       const float* __restrict__ spectrum, RasterParams p,
+                                                       float4* __restrict__ image) {
+    extern __shared__ float4 smem4[];
+    Rec* recs = (Rec*)smem4;
+    float* xyz = (float*)(recs + kBatchRecords);  // [maxW * WS][3]
+    float* blend = xyz + 3 * p.maxW * p.WS;       // [WS]
+
+    const int tile = blockIdx.x;
+    const int tx = tile % p.ntx, ty = tile / p.ntx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        const float sub_step = 1.0f / (float)p.WS;
+        float b = 0.0f;
+        for (int i = 0; i < p.WS; i++) {
+            blend[i] = b;
+            b += sub_step;
+        }
+    }
+    if (p.W > 1) {
+        const float sub_step = 1.0f / (float)p.WS;
+        const float wl_step = sub_step / (float)p.W;
+        for (int w = threadIdx.x; w < p.maxW; w += kThreads) {
+            float pos = ((float)w + 0.5f) / (float)p.W;
+            for (int i = 0; i < p.WS; i++) {
+                for (int c = 0; c < 3; c++)
+                    xyz[3 * (w * p.WS + i) + c] = sample_linear(spectrum, RF_SPECTRUM_WIDTH, 1, 4, c, pos, 0.0f, true);
+                pos += wl_step;
+            }
+        }
+    }
+
+    const int S = p.S;
+    const float inv_scale = 1.0f / p.ghost_scale;
+    // per-thread accumulators of the four pixels, [k * 3 + channel][thread]
+    float* acc = blend + ((p.WS + 3) & ~3);
+#pragma unroll
+    for (int c = 0; c < 12; c++) acc[c * kThreads + threadIdx.x] = 0.0f;
+
+    const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
+    const int per_batch = kBatchRecords / p.WS;  // entries per batch (WS <= kBatchRecords)
+    // thread j loads corner j % 4 of entry j / 4 of the batch; the next batch is
+    // prefetched into registers while the current one is shaded
+    const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
+    CornerLoad next[kBatchRecords / 64];
+    bool have_next[kBatchRecords / 64];
+#pragma unroll
+    for (int h = 0; h < kBatchRecords / 64; h++) {
+        const int e = my_entry + 64 * h;
+        have_next[h] = e < per_batch && begin + e < end;
+        if (have_next[h]) load_corner(vtx, tile_entries[begin + e], my_corner, p, next[h]);
+    }
+    for (uint32_t base = begin; base < end; base += per_batch) {
+        const int n_entries = (int)min((uint32_t)per_batch, end - base);
+        const int n_rec = n_entries * p.WS;
+        __syncthreads();  // the previous batch is shaded
+#pragma unroll
+        for (int h = 0; h < kBatchRecords / 64; h++) {
+            const int e = my_entry + 64 * h;
+            if (have_next[h])
+                for (int i = 0; i < p.WS; i++) store_corner(next[h], my_corner, blend[i], S, recs[e * p.WS + i]);
+            have_next[h] = e < per_batch && base + per_batch + e < end;
+            if (have_next[h]) load_corner(vtx, tile_entries[base + per_batch + e], my_corner, p, next[h]);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n_rec; j += kThreads) {
+            const uint32_t entry = tile_entries[base + j / p.WS];
+            finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int k = 0; k < 4; k++) {
+            const int blk = warp + 8 * k;
+            const int x0 = tx * kTile + (blk & 3) * 8, y0 = ty * kTile + (blk >> 2) * 4;
+            const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
+            const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
+            const bool in_image = px < p.width && py < p.height;
+            const int sx0 = px * S, sy0 = py * S;
+            // which records can touch this 8 x 4 block: lanes test 32 records at a time
+            unsigned sel[kBatchRecords / 32];
+#pragma unroll
+            for (int m = 0; m < kBatchRecords / 32; m++) {
+                const int j = m * 32 + lane;
+                bool take = false;
+                if (j < n_rec) {
+                    const Rec& r = recs[j];
+                    const int flags = r.flags;
+                    if (!(flags & 2)) {  // both triangles collinear: intersect_quad rejects all
+                        const int4 bb = *reinterpret_cast<const int4*>(r.bb);
+                        take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);
+                    }
+                }
+                sel[m] = __ballot_sync(0xffffffffu, take);
+            }
+            float r0 = acc[(3 * k) * kThreads + threadIdx.x];
+            float r1 = acc[(3 * k + 1) * kThreads + threadIdx.x];
+            float r2 = acc[(3 * k + 2) * kThreads + threadIdx.x];
+#pragma unroll
+            for (int m = 0; m < kBatchRecords / 32; m++) {
+                unsigned bits = sel[m];
+                while (bits) {  // in increasing record order: the reference's summation order
+                    const int j = m * 32 + __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const Rec& r = recs[j];
+                    if (!in_image) continue;
+                    if (r.flags & 1) {
+                        const int4 bb = *reinterpret_cast<const int4*>(r.bb);
+                        if (sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w) continue;
+                    }
+                    int hits = 0;
+                    for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
+                    if (hits == 0) continue;
+                    float wt[4];
+                    barycentric_fast(r.q, sx0 + S / 2, sy0 + S / 2, wt);
+                    const float f = fragment_fast(r, wt, ghost, p, inv_scale, hits);
+                    if (p.W > 1) {
+                        const float* c = xyz + 3 * r.color;
+                        r0 += c[0] * f;
+                        r1 += c[1] * f;
+                        r2 += c[2] * f;
+                    } else {
+                        r0 += f;
+                        r1 += f;
+                        r2 += f;
+                    }
+                }
+            }
+            acc[(3 * k) * kThreads + threadIdx.x] = r0;
+            acc[(3 * k + 1) * kThreads + threadIdx.x] = r1;
+            acc[(3 * k + 2) * kThreads + threadIdx.x] = r2;
+        }
+    }
+
+    const float scale = p.intensity / (float)(p.W * p.S * p.WS);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int blk = warp + 8 * k;
+        const int px = tx * kTile + (blk & 3) * 8 + (lane & 7), py = ty * kTile + (blk >> 2) * 4 + (lane >> 3);
+        if (px >= p.width || py >= p.height) continue;
+        const float c0 = acc[(3 * k) * kThreads + threadIdx.x], c1 = acc[(3 * k + 1) * kThreads + threadIdx.x],
+                    c2 = acc[(3 * k + 2) * kThreads + threadIdx.x];
+        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c0 > 0.0f || c1 > 0.0f || c2 > 0.0f) out = xyz_to_ap1(c0 * scale, c1 * scale, c2 * scale);
+        image[(size_t)(p.height - (py + 1)) * p.width + px] = out;
+    }
+}
+
+// The reference's own loop: every pixel scans every mask of its bin (rasterizing.cl:573-654).
+__global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__ vtx,
+                                                      const unsigned long long* __restrict__ masks, int batch_count,
+                                                      int B, long long prim_total, const float* __restrict__ ghost,
+                                                      const float* __restrict__ spectrum, RasterParams p,
+                                                      float4* __restrict__ image) {
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    if (x >= p.width || y >= p.height) return;
+    const int bdx = (p.width + B - 1) / B;
+    const int bin = (y / B) * bdx + (x / B);
+    const int S = p.S;
+    const int sx0 = x * S, sy0 = y * S;
+    const float sub_step = 1.0f / (float)p.WS;
+    const float wl_step = sub_step / (float)p.W;
+    const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
+    float rgb[3] = {0.f, 0.f, 0.f};
+    Rec r;
+    for (int batch = 0; batch < batch_count; batch++) {
+        const unsigned long long* q = masks + 4 * ((size_t)bin * batch_count + batch);
+        if ((q[0] & 1ull) == 0) continue;
+        for (int k = 0; k < RF_BATCH_PRIMITIVE_COUNT; k++) {
+            const long long prim = (long long)batch * RF_BATCH_PRIMITIVE_COUNT + k;
+            if (prim >= prim_total) continue;
+            const int bit = k + 1;
+            if (!((q[bit >> 6] >> (bit & 63)) & 1ull)) continue;
+            const long long path = prim / Q;
+            const int quad = (int)(prim % Q);
+            const int row = quad / (p.G - 1), col = quad % (p.G - 1);
+            const int c0 = row * p.G + col;
+            const int corners[4] = {c0, c0 + 1, c0 + 1 + p.G, c0 + p.G};
+            for (int w = 0; w < p.maxW; w++) {
+                float sub_pos = 0.0f;
+                float wl_pos = ((float)w + 0.5f) / (float)p.W;
+                for (int i = 0; i < p.WS; i++) {
+                    // the full record, no skipping of invalid endpoints
+                    for (int c = 0; c < 4; c++) {
+                        const long long vi = (path * VC + corners[c]) * p.W + w;
+                        const float4 a0 = vtx[2 * vi], a1 = vtx[2 * vi + 1], b0 = vtx[2 * vi + 2], b1 = vtx[2 * vi + 3];
+                        const float px = a0.x + (b0.x - a0.x) * sub_pos, py = a0.y + (b0.y - a0.y) * sub_pos;
+                        r.uv[2 * c] = a0.z + (b0.z - a0.z) * sub_pos;
+                        r.uv[2 * c + 1] = a0.w + (b0.w - a0.w) * sub_pos;
+                        r.rrel[c] = a1.x + (b1.x - a1.x) * sub_pos;
+                        r.refl[c] = a1.y + (b1.y - a1.y) * sub_pos;
+                        r.inten[c] = a1.z + (b1.z - a1.z) * sub_pos;
+                        r.q[2 * c] = cvt_rz_sat(px * (float)S);
+                        r.q[2 * c + 1] = cvt_rz_sat(py * (float)S);
+                    }
+                    const int* qq = r.q;
+                    edge_coeffs(qq[0], qq[1], qq[2], qq[3], r.ec + 0);
+                    edge_coeffs(qq[2], qq[3], qq[4], qq[5], r.ec + 3);
+                    edge_coeffs(qq[4], qq[5], qq[6], qq[7], r.ec + 6);
+                    edge_coeffs(qq[6], qq[7], qq[0], qq[1], r.ec + 9);
+                    edge_coeffs(qq[4], qq[5], qq[0], qq[1], r.ec + 12);
+                    const bool never = edge_i(qq[0], qq[1], qq[2], qq[3], qq[4], qq[5]) == 0 &&
+                                       edge_i(qq[0], qq[1], qq[4], qq[5], qq[6], qq[7]) == 0;
+                    int hits = 0;
+                    if (!never)
+                        for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
+                    float f = 0.0f;
+                    if (hits > 0) {
+                        float wt[4];
+                        barycentric_fast(r.q, sx0 + S / 2, sy0 + S / 2, wt);
+                        f += fragment_fast(r, wt, ghost, p, 1.0f / p.ghost_scale, hits);
+                    }
+                    if (p.W > 1) {
+                        for (int c = 0; c < 3; c++)
+                            rgb[c] += sample_linear(spectrum, RF_SPECTRUM_WIDTH, 1, 4, c, wl_pos, 0.0f, true) * f;
+                    } else {
+                        rgb[0] += f;
+                        rgb[1] += f;
+                        rgb[2] += f;
+                    }
+                    sub_pos += sub_step;
+                    wl_pos += wl_step;
+                }
+            }
+        }
+    }
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (rgb[0] > 0.0f || rgb[1] > 0.0f || rgb[2] > 0.0f) {
+        const float scale = p.intensity / (float)(p.W * p.S * p.WS);
+        out = xyz_to_ap1(rgb[0] * scale, rgb[1] * scale, rgb[2] * scale);
+    }
+    image[(size_t)(p.height - (y + 1)) * p.width + x] = out;
+}
+
+bool make_params(const rf_raster_args& a, RasterParams& p) {
+    if (a.width < 1 || a.height < 1 || a.grid_count < 2 || a.wavelength_count < 1 || a.wavelength_sub_count < 1 ||
+        a.path_count < 0 || a.ghost_width < 1 || a.ghost_height < 1)
+        return false;
+    if (a.sub_steps != 1 && a.sub_steps != 2 && a.sub_steps != 4 && a.sub_steps != 8) return false;
+    p.width = a.width;
+    p.height = a.height;
+    p.S = a.sub_steps;
+    p.W = a.wavelength_count;
+    p.WS = a.wavelength_sub_count;
+    p.G = a.grid_count;
+    p.maxW = a.wavelength_count - 1 > 1 ? a.wavelength_count - 1 : 1;
+    p.intensity = a.intensity;
+    p.ghost_scale = a.ghost_scale;
+    p.ghost_w = a.ghost_width;
+    p.ghost_h = a.ghost_height;
+    p.safe_screen = (float)a.width * a.sub_steps <= 16384.0f && (float)a.height * a.sub_steps <= 16384.0f;
+    return true;
+}
+
+int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
+                  const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
+    p.T = kTile;
+    p.ntx = (p.width + kTile - 1) / kTile;
+    const int nty = (p.height + kTile - 1) / kTile;
+    const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
+                        sizeof(float) * 12 * kThreads;
+    if (smem > 48 * 1024)
+        RF_TRY(cuda_status(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
+    k_raster<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum, p,
+                                                (float4*)image);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace rf
+
+extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                         const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
+                         void* stream) {
+    using namespace rf;
+    if (!vertexes || !tile_offsets || !ghost || !spectrum || !args || !image) return RF_ERR_INVALID_ARG;
+    if (!aligned16(vertexes) || !aligned16(image)) return RF_ERR_INVALID_ARG;
+    RasterParams p;
+    if (!make_params(*args, p)) return RF_ERR_INVALID_ARG;
+    if (p.WS > kBatchRecords || p.maxW * p.WS > 4096) return RF_ERR_INVALID_ARG;
+    if (tile_size_of(*args) != kTile) return RF_ERR_NOT_SUPPORTED;
+    return launch_raster(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image, (cudaStream_t)stream);
+}
+
+extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_count, const float* ghost,
+                               const float* spectrum, const rf_raster_args* args, float* image, void* stream) {
+    using namespace rf;
+    if (!vertexes || !masks || !ghost || !spectrum || !args || !image || batch_count < 0) return RF_ERR_INVALID_ARG;
+    RasterParams p;
+    if (!make_params(*args, p)) return RF_ERR_INVALID_ARG;
+    const long long prim_total = (long long)args->path_count * (args->grid_count - 1) * (args->grid_count - 1);
+    dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
+    k_raster_masks<<<grid, 256, 0, (cudaStream_t)stream>>>((const float4*)vertexes, (const unsigned long long*)masks,
+                                                           batch_count, args->bin_size, prim_total, ghost, spectrum,
+                                                           p, (float4*)image);
+    return launch_status();
+}

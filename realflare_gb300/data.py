@@ -235,6 +235,9 @@ class FlareLens:
     coating_layer_ior: tuple = (1.38, 1.65)
     # A lens model can be given directly instead of by path (synthetic lenses).
     lens_model: Any = None
+    # Explicit ghost paths ((bounce1, bounce2) element pairs); empty = the reference's
+    # ray_paths (same-side pairs).
+    ghost_paths: tuple = field(default_factory=tuple)
 
 
 @_hashable

@@ -40,6 +40,10 @@ def trace_inputs(project: Project, paths=None, path_indexes: tuple = ()) -> Trac
     )
     if len(elements) <= 1:
         return None
+    if paths is None and lens.ghost_paths:
+        paths = list(lens.ghost_paths)
+        if path_indexes:
+            paths = [pp for i, pp in enumerate(paths) if i in path_indexes]
     if paths is None:
         paths = lens_mod.ray_paths(model, tuple(path_indexes))
     paths = np.asarray(paths, np.int32).reshape(-1, 2)

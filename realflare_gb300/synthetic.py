@@ -181,4 +181,6 @@ def workload(name: str, integer_wavelengths: bool = False) -> Workload:
         raise KeyError(name)
     if integer_wavelengths:
         p.render.wavelengths = tuple(float(int(round(w))) for w in p.render.wavelengths)
-    return Workload(name, p, lens_mod.all_two_bounce_paths(model))
+    paths = lens_mod.all_two_bounce_paths(model)
+    p.flare.lens.ghost_paths = tuple(tuple(pp) for pp in paths)
+    return Workload(name, p, paths)
