@@ -277,11 +277,13 @@ class CpuBaseline:
     The whole frame's inputs (rays, primitives, vertices, bin masks, ghost texture,
     starburst spectrum) are computed once on the host, untimed; ``measure()`` then times,
     per stage: the trace, prim and vertex shaders of 2 ghosts and the binner on their
-    primitives (scaled by ghosts), the rasteriser on 4 spans of 64 pixels (scaled by
-    pixels), one starburst row (scaled by rows), and the numpy FFT stages whole.
+    primitives (scaled by ghosts), the rasteriser on a stratified sample of pixels (a span
+    of SPAN pixels at the centre of each cell of a GRID x GRID grid over the image, scaled
+    by pixels), one starburst row (scaled by rows), and the numpy FFT stages whole.
     """
 
-    SPAN = 64
+    SPAN = 16
+    GRID = 4
 
     def __init__(self, workload) -> None:
         import numpy as np
@@ -363,7 +365,9 @@ class CpuBaseline:
         out['setup_bin'] = (time.perf_counter() - t0) * P / 2
         h, w = ra.height, ra.width
         t_r = 0.0
-        spans = [(h // 8, w // 8), (3 * h // 8, 5 * w // 8), (5 * h // 8, 3 * w // 8), (7 * h // 8, 7 * w // 8)]
+        g = self.GRID
+        spans = [((2 * j + 1) * h // (2 * g), (2 * i + 1) * w // (2 * g) - self.SPAN // 2)
+                 for j in range(g) for i in range(g)]
         for y, x in spans:
             t0 = time.perf_counter()
             if ref is not None:
@@ -404,8 +408,9 @@ class CpuBaseline:
             'cores': os.cpu_count(),
             'kind': self.kind,
             'sample': (f'one frame of this workload: trace, prim/vertex shaders and binner on 2 of '
-                       f'{self.P} ghosts, rasteriser on 4 spans of {self.SPAN} pixels, 1 starburst row, numpy '
-                       f'FFT stages whole; each stage scaled to the whole frame'),
+                       f'{self.P} ghosts, rasteriser on {self.GRID * self.GRID} spans of {self.SPAN} pixels (one '
+                       f'per cell of a {self.GRID}x{self.GRID} grid), 1 starburst row, numpy FFT stages whole; '
+                       f'each stage scaled to the whole frame'),
             'stage_seconds': {k: round(v, 3) for k, v in stages.items()},
             'rays_per_s': self.n_rays / stages['trace'],
         }
