@@ -19,7 +19,8 @@ Lens acceptance: random radii with random signs often give a system that no ray 
 (at seed 0, 0.6 % of the 16-surface lens's ghost rays and 1.8 % of the 24-surface lens's
 reach the sensor). The workloads therefore use, per surface count, the first seed
 0, 1, 2, ... whose two-bounce ghost rays reach the sensor for at least
-``ACCEPT_FRACTION`` of a 12 x 12 grid over ``GRID_LENGTH`` at 550 nm (light on axis).
+``ACCEPT_FRACTION`` of a 12 x 12 grid over ``GRID_LENGTH`` at 550 nm with the
+workload's light position.
 ``LENS_SEEDS`` records the result of that rule (checked by the CPU tests); the 8-surface
 lens is accepted at seed 0.
 """

@@ -208,3 +208,31 @@ def test_render_path_matches_oracle(oracle, key):
     image = RasterizingTask().run(w.project, rays, Image(tensor=dev(ghost)))
     got = image.array
     assert rel_l2(got, r['image']) < IMAGE_RTOL
+
+
+@pytest.mark.parametrize('name', ['plain8_g12_96', 'spectral16_g10_64'])
+def test_cuda_path_reproduces_golden_vectors(name):
+    """The CUDA stages on the inputs of the reference-generated golden fixtures."""
+    import os
+
+    from golden.make_golden import case_project
+
+    with np.load(os.path.join(os.path.dirname(__file__), 'golden', f'{name}.npz')) as z:
+        g = {k: z[k] for k in z.files}
+    w = case_project(name)
+    ti = prepare.trace_inputs(w.project, w.paths)
+    got = gpu_trace(ti)
+    for k in range(5):
+        np.testing.assert_array_equal(np.nan_to_num(got[k], nan=9e9), np.nan_to_num(g['rays'][k], nan=9e9))
+    assert (np.isnan(got[5]) == np.isnan(g['rays'][5])).all()
+    a = ti.args
+    P, W, G = a.path_count, a.wavelength_count, a.grid_count
+    ra = prepare.raster_args(w.project, P, W, g['ghost'].shape)
+    bounds_d, vtx_d = dev(g['bounds']), dev(g['vertexes'])
+    offsets, entries, task = gpu_tiles(ra, bounds_d, vtx_d)
+    image = torch.empty((ra.height, ra.width, 4), device='cuda')
+    ghost_d, spec_d = dev(g['ghost']), dev(light_spectrum())
+    check(lib().rf_raster(vtx_d.data_ptr(), offsets.data_ptr(), entries.data_ptr(), ghost_d.data_ptr(),
+                          spec_d.data_ptr(), ctypes.byref(ra), image.data_ptr(), stream()), 'rf_raster')
+    torch.cuda.synchronize()
+    assert rel_l2(image.cpu().numpy(), g['image']) < STAGE_RTOL

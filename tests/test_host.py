@@ -1,0 +1,127 @@
+"""Host-side logic: glass catalogue (the reference's own known-answer tests), lens element
+construction, ghost paths, wavelengths, synthetic lenses and argument preparation."""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+from realflare_gb300 import glass, lens, prepare, synthetic
+from realflare_gb300.constants import LAMBDA_MAX, LAMBDA_MIN, light_spectrum
+from realflare_gb300.data import Glass, LensElement, LensModel, Project, QSize, RealflareError, cast
+
+REFERENCE = os.environ.get('REALFLARE_REFERENCE', '/root/reference')
+
+
+def test_glass_catalogue_known_answers():
+    # realflare tests/glass.py:11-53
+    glasses = glass.glasses_from_path('$GLASS/schott')
+    assert glasses[0] == Glass('BAFN6', 'schott', 1.589, 48.45,
+                               [1.36719201, 0.00882820704, 0.10907994, 0.0438731646, 1.02108011, 113.58602])
+    closest = glass.closest_glass(tuple(glasses), 1.5, 80, 0)
+    assert closest == Glass('N-PK52A', 'schott', 1.497, 81.61,
+                            [1.029607, 0.00516800155, 0.1880506, 0.0166658798, 0.736488165, 138.964129])
+    assert glass.manufacturers() == {'schott': '$GLASS/schott'}
+    assert glass.closest_glass((), 1.5, 60) is None and glass.closest_glass(tuple(glasses), 0, 60) is None
+
+
+def test_sellmeier_matches_catalogue_nd():
+    for g in glass.glasses_from_path('$GLASS/schott')[:40]:
+        assert abs(glass.sellmeier(g.coefficients, 587.5618) - g.n) < 2e-3
+
+
+def test_lens_elements_follow_reference_rules():
+    m = LensModel(aperture_index=1, lens_elements=[
+        LensElement(radius=50, distance=5, refractive_index=1.6, abbe_nr=40, height=12),
+        LensElement(radius=0, distance=3, refractive_index=1.0, height=8),
+        LensElement(radius=-40, distance=30, refractive_index=1.0, height=12)])
+    el = lens.elements(m, (36, 24), '$GLASS/schott', 0, (550, 0, 600))
+    assert len(el) == 4  # + sensor
+    assert list(el['center']) == [50, 5, 8 - 40, 38]  # sum(distance before) + radius
+    assert el[3]['height'] == pytest.approx(math.hypot(36, 24) / 2)
+    assert list(el['coating']) == [550, 0, 600, 0]
+    assert not np.isnan(el[0]['coefficients'][0])
+    el2 = lens.elements(m, (36, 24), '/nonexistent', 0, ())
+    assert np.isnan(el2[0]['coefficients'][0])  # no catalogue: dispersion off (lens.py:61-62)
+
+
+def test_ray_paths_and_wavelengths():
+    m = LensModel(aperture_index=3, lens_elements=[LensElement()] * 8)
+    paths = lens.ray_paths(m)
+    assert paths == [(1, 0), (2, 0), (2, 1), (5, 4), (6, 4), (6, 5)]
+    assert lens.ray_paths(m, (1, 4)) == [(2, 0), (6, 4)]
+    assert lens.ray_paths(m, (-1,)) == [(-1, -1)]
+    assert len(lens.all_two_bounce_paths(synthetic.make_lens(24, 11))) == 276
+    wl = lens.wavelength_array(4)
+    assert wl == [LAMBDA_MIN + (i + 0.5) / 4 * (LAMBDA_MAX - LAMBDA_MIN) for i in range(4)]
+    assert light_spectrum().shape == (340, 4)
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, 'realflare')), reason='reference checkout absent')
+def test_real_lens_models_ghost_counts():
+    counts = {'Canon': 304, 'Kodak': 25, 'Leica': 36, 'Tronnier': 11, 'Zeiss': 127}
+    root = os.path.join(REFERENCE, 'realflare', 'resources', 'model')
+    for maker, n in counts.items():
+        d = os.path.join(root, maker)
+        f = os.path.join(d, sorted(os.listdir(d))[0])
+        assert len(lens.ray_paths(lens.model_from_path(f))) == n, maker
+
+
+def test_model_errors():
+    with pytest.raises(RealflareError):
+        lens.model_from_path('')
+    with pytest.raises(RealflareError):
+        lens.model_from_path('/nonexistent/lens.json')
+
+
+def test_project_cast_and_hash():
+    p = cast(Project, {'render': {'resolution': [640, 480], 'grid_count': 17},
+                       'flare': {'lens': {'coating': [500, 600], 'sensor_size': [36, 24]}}})
+    assert p.render.resolution.width() == 640 and p.render.grid_count == 17
+    assert p.flare.lens.coating == (500, 600)
+    assert hash(p) == hash(cast(Project, {'render': {'resolution': [640, 480], 'grid_count': 17},
+                                          'flare': {'lens': {'coating': [500, 600], 'sensor_size': [36, 24]}}}))
+
+
+def test_synthetic_lens_acceptance_rule():
+    """LENS_SEEDS is the first seed whose ghost rays reach the sensor at >= 40 %."""
+    from oracle.oracle import Oracle
+
+    o = Oracle('f32')
+
+    def fraction(n, seed):
+        w = synthetic.workload({8: 'plain-8', 16: 'spectral-16', 24: 'production-24'}[n])
+        m = synthetic.make_lens(n, seed)
+        w.project.flare.lens.lens_model = m
+        w.project.flare.lens.coating_thickness = ()
+        paths = lens.all_two_bounce_paths(m)
+        w.project.render.grid_count = 12
+        w.project.render.wavelengths = (550.0,)
+        ti = prepare.trace_inputs(w.project, paths)
+        r = o.trace(ti.elements, ti.paths, ti.wavelengths, ti.args)
+        return np.isfinite(r[5]).mean()
+
+    for n, seed in synthetic.LENS_SEEDS.items():
+        assert fraction(n, seed) >= synthetic.ACCEPT_FRACTION
+        for s in range(seed):
+            assert fraction(n, s) < synthetic.ACCEPT_FRACTION
+
+
+def test_prepare_arguments():
+    w = synthetic.workload('production-24')
+    ti = prepare.trace_inputs(w.project)
+    assert ti.args.path_count == 276 and ti.args.wavelength_count == 16 and ti.args.grid_count == 128
+    assert ti.ray_count == 276 * 16 * 128 * 128
+    assert ti.elements['coating_layers'].tolist()[:3] == [2, 2, 2]
+    ra = prepare.raster_args(w.project, 276, 16, (256, 256))
+    assert ra.screen_transform == pytest.approx(2048 / (math.hypot(36, 24) / 2))
+    assert ra.intensity == pytest.approx(1e3)
+    w.project.render.anti_aliasing = 3
+    with pytest.raises(RealflareError):
+        prepare.raster_args(w.project, 276, 16, (256, 256))
+    p = Project()
+    p.render.resolution = QSize(100, 50)
+    d = lens.direction((0.5, -0.5), p.render.resolution, (36, 24), 50)
+    assert list(d) == pytest.approx([9.0, -4.5, 50, 1])

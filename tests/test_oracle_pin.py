@@ -1,0 +1,84 @@
+"""The C oracle against the reference's own OpenCL kernels compiled for the host
+(oracle/_ref, built from the reference checkout or its generated sources): bit-identical
+rays, primitive bounds and intensities, vertices, bin masks and images on reduced 8-, 16-
+and 24-surface workloads, and the same aperture masks and starburst images."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import ghost_texture, reduced
+
+from realflare_gb300 import prepare
+from realflare_gb300.constants import light_spectrum
+
+oracle_mod = pytest.importorskip('oracle.oracle')
+if not oracle_mod.reference_available():
+    pytest.skip('reference kernels not available (no checkout and no generated sources)',
+                allow_module_level=True)
+
+CASES = {
+    'plain-8': dict(grid=20, resolution=128),
+    'spectral-16': dict(grid=16, resolution=128, paths=24, wavelengths=4),
+    # the reference has single-layer coatings only: its lambda0 rule is used here
+    'production-24': dict(grid=12, resolution=128, paths=24, wavelengths=5),
+}
+
+
+@pytest.fixture(scope='module')
+def pair():
+    return oracle_mod.Oracle('f32'), oracle_mod.Reference()
+
+
+def nan_equal(a, b):
+    return np.array_equal(np.nan_to_num(a, nan=7e30), np.nan_to_num(b, nan=7e30))
+
+
+@pytest.mark.parametrize('name', list(CASES))
+def test_oracle_bit_identical_to_reference_kernels(pair, name):
+    o, r = pair
+    w = reduced(name, **CASES[name])
+    w.project.flare.lens.coating_thickness = ()
+    ti = prepare.trace_inputs(w.project, w.paths)
+    a = ti.args
+    P, W, G = a.path_count, a.wavelength_count, a.grid_count
+    rays_o = o.trace(ti.elements, ti.paths, ti.wavelengths, a)
+    rays_r = r.trace(ti.elements, ti.paths, ti.wavelengths.astype(np.int32), a)
+    assert nan_equal(rays_o, rays_r)
+    area, min_area = prepare.quad_constants(w.project)
+    bo, io = o.quad_setup(rays_r, P, W, G, area, min_area)
+    br, ir = r.prim_shader(rays_r, P, W, G, area, min_area)
+    assert nan_equal(bo, br) and nan_equal(io, ir)
+    ghost = ghost_texture((48, 48), seed=3)
+    ra = prepare.raster_args(w.project, P, W, ghost.shape)
+    vo = o.vertex(rays_r, ir, P, W, G, ra.screen_transform, ra.width, ra.height)
+    vr = r.vertex_shader(rays_r, ir, P, W, G, ra.screen_transform, ra.width, ra.height)
+    assert nan_equal(vo, vr)
+    mo = o.bin_masks(br, ra.screen_transform, ra.width, ra.height, ra.bin_size)
+    mr = r.binner(br, ra.screen_transform, ra.width, ra.height, ra.bin_size, local_size=64)
+    assert np.array_equal(mo, mr)
+    io_ = o.raster(vr, mr, ghost, light_spectrum(), ra)
+    ir_ = r.rasterizer(vr, mr, ghost, light_spectrum(), ra)
+    assert np.array_equal(io_, ir_)
+    assert (ir_[..., :3] != 0).any()
+
+
+def test_aperture_and_starburst_match_reference_kernels(pair):
+    o, r = pair
+    for blades, rot, rnd, soft in [(6, 0.0, 0.0, 0.0), (8, 0.4, 0.3, 0.03)]:
+        assert np.array_equal(o.aperture_shape(64, 48, (0.75, 0.6), blades, rot, rnd, soft),
+                              r.aperture_shape(64, 48, (0.75, 0.6), blades, rot, rnd, soft))
+    base = o.aperture_shape(64, 64, (0.75, 0.75), 8, 0.0, 0.0, 0.0)
+    assert np.array_equal(o.aperture_dust(base, (0.75, 0.75), 0.7, 0.3, 0.05, (0.1, 0.2), 0.02),
+                          r.aperture_dust(base, (0.75, 0.75), 0.7, 0.3, 0.05, (0.1, 0.2), 0.02))
+    spec = oracle_mod.fft_power_spectrum(base, 560e-6, 1000.0).astype(np.float32)
+    from realflare_gb300._abi import StarburstArgs
+
+    a = StarburstArgs()
+    a.width, a.height, a.spectrum_width, a.spectrum_height, a.spectrum_count = 48, 40, 64, 64, 1
+    a.samples, a.blur, a.rotation, a.rotation_weight = 24, 0.02, 0.3, 1.5
+    a.vignetting[0], a.vignetting[1] = 0.75, 1.0
+    a.intensity = 1e-6
+    a.offset[0], a.offset[1] = 0.2, -0.1
+    a.scale[0], a.scale[1] = 1.0, 1.2
+    assert np.array_equal(o.starburst(spec, light_spectrum(), a), r.starburst(spec, light_spectrum(), a))
