@@ -84,7 +84,8 @@ typedef struct rf_raster_args {
 
 /* ---- library ---------------------------------------------------------------------- */
 const char* rf_version(void);
-/* Text of the last CUDA error seen by this thread (empty if none). */
+/* Text of the last CUDA error (or rejected argument, where a function says so) seen by
+ * this thread; empty if none. */
 const char* rf_last_cuda_error(void);
 /* Number of kernels this library has launched in this process (all threads). */
 long long rf_launch_count(void);
@@ -208,6 +209,22 @@ int rf_starburst(const float* spectrum, const float* light_spectrum, const rf_st
  * complex64[3][h][w]. */
 int rf_ghost_frft(const float* aperture, int32_t width, int32_t height, float alpha,
                   float* scratch, float* texture, void* stream);
+
+/* Largest width * height that rf_ghost_frft_static accepts (512 x 512 pixels). */
+#define RF_GHOST_FRFT_STATIC_MAX_PIXELS (512 * 512)
+
+/* rf_ghost_frft for callers that cannot allocate device memory: it has no counterpart in
+ * the reference. A plugin inside a host application that owns all device memory through
+ * its own pool, or a render loop that must not allocate after start-up (an allocation can
+ * synchronise the device and stall a frame), passes only the aperture and the texture;
+ * the scratch is a static device array of 3 x RF_GHOST_FRFT_STATIC_MAX_PIXELS complex64
+ * values (6 MiB) that every GPU loading this library holds until the process exits. The
+ * first call on a device looks up the array's device address, so make that first call
+ * before any stream capture. All calls share the array: calls that overlap on the GPU
+ * (other streams, other host threads on the same device) race. Sizes above the maximum
+ * return RF_ERR_INVALID_ARG (text via rf_last_cuda_error). Allocates nothing. */
+int rf_ghost_frft_static(const float* aperture, int32_t width, int32_t height, float alpha,
+                         float* texture, void* stream);
 
 /* ---- aperture masks ----------------------------------------------------------------- */
 /* aperture_shape kernel (realflare/api/tasks/cl/aperture.cl:5-47): writes image[h][w]. */

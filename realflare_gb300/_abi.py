@@ -105,6 +105,7 @@ SIGNATURES = {
     'rf_starburst_spectrum': [P, I32, I32, ctypes.POINTER(F32), I32, F32, P, P, P],
     'rf_starburst': [P, P, ctypes.POINTER(StarburstArgs), P, P],
     'rf_ghost_frft': [P, I32, I32, F32, P, P, P],
+    'rf_ghost_frft_static': [P, I32, I32, F32, P, P],
     'rf_aperture_shape': [P, I32, I32, F32, F32, I32, F32, F32, F32, P],
     'rf_aperture_dust': [P, I32, I32, F32, F32, F32, F32, F32, F32, F32, F32, P],
     'rf_aperture_noise_dust': [P, P, P, I32, I32, F32, F32, P],

@@ -11,6 +11,7 @@ namespace {
 thread_local char g_last_error[256] = "";
 std::atomic<long long> g_launches{0};
 }  // namespace
+void set_error_text(const char* text) { snprintf(g_last_error, sizeof g_last_error, "%s", text); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void set_cuda_error(cudaError_t e) {
     const char* name = cudaGetErrorName(e);

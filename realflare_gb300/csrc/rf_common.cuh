@@ -12,6 +12,7 @@ namespace rf {
 
 // ---------------------------------------------------------------- host error plumbing
 void set_cuda_error(cudaError_t e);
+void set_error_text(const char* text);
 void count_launch();
 // Called after every kernel launch: counts it and reports a launch error.
 inline int launch_status() {

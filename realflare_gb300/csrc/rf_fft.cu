@@ -263,3 +263,55 @@ extern "C" int rf_ghost_frft(const float* aperture, int32_t width, int32_t heigh
                                          (float)std::sqrt((double)n));
     return launch_status();
 }
+
+// ---------------------------------------------------------------- no-allocation variant
+//
+// Some callers cannot allocate device memory at render time: a plugin inside a host
+// application that owns every device allocation through its own pool (and forbids
+// cudaMalloc in its render callback), or a real-time loop that must not allocate after
+// start-up because an allocation can synchronise the device and stall a frame. For them,
+// rf_ghost_frft_static keeps its scratch in this file-scope device array instead of a
+// caller buffer. Every GPU that loads the library holds the array (6 MiB) until the
+// process exits; all calls share it.
+#include <mutex>
+
+static __device__ __align__(256) float2 g_ghost_frft_scratch[3 * RF_GHOST_FRFT_STATIC_MAX_PIXELS];
+
+namespace rf {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+float* g_static_scratch[kMaxDevices] = {};
+
+// Device address of the static scratch on the current device, looked up on the first
+// call for each device (the host-side symbol is not a device address).
+int static_scratch(float** out) {
+    int dev = 0;
+    RF_TRY(cuda_status(cudaGetDevice(&dev)));
+    if (dev < 0 || dev >= kMaxDevices) return RF_ERR_NOT_SUPPORTED;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_scratch[dev]) {
+        void* p = nullptr;
+        RF_TRY(cuda_status(cudaGetSymbolAddress(&p, g_ghost_frft_scratch)));
+        g_static_scratch[dev] = (float*)p;
+    }
+    *out = g_static_scratch[dev];
+    return RF_OK;
+}
+}  // namespace
+}  // namespace rf
+
+extern "C" int rf_ghost_frft_static(const float* aperture, int32_t width, int32_t height, float alpha,
+                                    float* texture, void* stream) {
+    using namespace rf;
+    if (!aperture || !texture || width < 1 || height < 1) return RF_ERR_INVALID_ARG;
+    if ((long long)width * height > RF_GHOST_FRFT_STATIC_MAX_PIXELS) {
+        set_error_text("rf_ghost_frft_static: width * height exceeds RF_GHOST_FRFT_STATIC_MAX_PIXELS (512 x 512)");
+        return RF_ERR_INVALID_ARG;
+    }
+    float* scratch = nullptr;
+    RF_TRY(static_scratch(&scratch));
+    // every scratch plane is fully written before it is read, so the previous call's
+    // contents never need clearing
+    return rf_ghost_frft(aperture, width, height, alpha, scratch, texture, stream);
+}
