@@ -30,7 +30,19 @@ int tile_size_of(const rf_raster_args& a);
 
 namespace {
 
-constexpr int kBatchRecords = 128;
+// Tuning knobs (compile-time): records per shared-memory batch, resident blocks per SM
+// requested from the register allocator, and where the half-angle tangents use the
+// reference's exact FP32 operations (1: small angles, 0: only a_i == 0).
+#ifndef RF_RASTER_BATCH
+#define RF_RASTER_BATCH 128
+#endif
+#ifndef RF_RASTER_MIN_BLOCKS
+#define RF_RASTER_MIN_BLOCKS 3
+#endif
+#ifndef RF_RASTER_EXACT_SMALL_ANGLES
+#define RF_RASTER_EXACT_SMALL_ANGLES 0
+#endif
+constexpr int kBatchRecords = RF_RASTER_BATCH;
 
 struct alignas(16) Rec {
     int bb[4];       // xmin, xmax, ymin, ymax (first: read as one 16-byte vector)
@@ -39,6 +51,7 @@ struct alignas(16) Rec {
     int flags;       // 1: bounds rejection is exact; 2: both triangles collinear (never inside)
     int color;       // w * WS + i
     float uv[8], rrel[4], inten[4], refl[4];
+    float qf[8];     // q as floats (exact: |q| < 2^24)
 };
 static_assert(sizeof(Rec) % 16 == 0 && offsetof(Rec, bb) == 0, "records are read with 16-byte loads");
 
@@ -80,128 +93,28 @@ __device__ __forceinline__ bool inside(const Rec& r, int px, int py) {
     return front || back;
 }
 
-// compute_barycentric_quad (rasterizing.cl:95-148)
-__device__ __forceinline__ void barycentric(const int* q, int px, int py, float w[4]) {
-    float sx[4], sy[4], a[4], d[4], r[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        sx[i] = (float)wsub(q[2 * i], px);
-        sy[i] = (float)wsub(q[2 * i + 1], py);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int j = (i + 1) & 3;
-        a[i] = sx[i] * sy[j] - sx[j] * sy[i];
-        d[i] = sx[i] * sx[j] + sy[i] * sy[j];
-        r[i] = sqrtf(sx[i] * sx[i] + sy[i] * sy[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        if (r[i] == 0.0f) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) w[k] = (k == i) ? 1.0f : 0.0f;
-            return;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-        if (a[i] == 0.0f) a[i] = 1e-3f;
-    float t[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) t[i] = (r[i] * r[(i + 1) & 3] - d[i]) / a[i];
-#pragma unroll
-    for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) / r[i];
-    const float sum = w[0] + w[1] + w[2] + w[3];
-#pragma unroll
-    for (int i = 0; i < 4; i++) w[i] = w[i] / sum;
-}
-
-// fragment_shader (rasterizing.cl:471-506) times the hit count
-__device__ __forceinline__ float fragment(const Rec& r, const float w[4], const float* __restrict__ ghost,
-                                          const RasterParams& p, int hits) {
-    float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
-    float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
-    u = (u / p.ghost_scale + 1.0f) / 2.0f;
-    v = (v / p.ghost_scale + 1.0f) / 2.0f;
-    const float gi = sample_linear(ghost, p.ghost_w, p.ghost_h, 1, 0, u, v, false);
-    const float rr = w[0] * r.rrel[0] + w[1] * r.rrel[1] + w[2] * r.rrel[2] + w[3] * r.rrel[3];
-    const float ri = smoothstepf(1.0f, 0.95f, rr);
-    float ai = w[0] * r.inten[0] + w[1] * r.inten[1] + w[2] * r.inten[2] + w[3] * r.inten[3];
-    float ci = w[0] * r.refl[0] + w[1] * r.refl[1] + w[2] * r.refl[2] + w[3] * r.refl[3];
-    ai = fmaxf(ai, 0.0f);
-    ci = fmaxf(ci, 0.0f);
-    return gi * ri * ai * ci * (float)hits;
-}
-
-// Expand entry (primitive, pair w) at sub step i into a record.
-__device__ void setup_record(const float4* __restrict__ vtx, uint32_t entry, int i, const float* blend,
-                             const RasterParams& p, Rec& r) {
-    const long long prim = entry / p.maxW;
-    const int w = (int)(entry % p.maxW);
-    const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
-    const long long path = prim / Q;
-    const int quad = (int)(prim % Q);
-    const int row = quad / (p.G - 1), col = quad % (p.G - 1);
-    const int c0 = row * p.G + col;
-    const int corners[4] = {c0, c0 + 1, c0 + 1 + p.G, c0 + p.G};
-    const float t = blend[i];
-    const float S = (float)p.S;
-    bool finite = true;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const long long vi = (path * VC + corners[k]) * p.W + w;
-        const float4 a0 = __ldg(vtx + 2 * vi), a1 = __ldg(vtx + 2 * vi + 1);
-        const float4 b0 = __ldg(vtx + 2 * vi + 2), b1 = __ldg(vtx + 2 * vi + 3);
-        // mix_vertex: x + (y - x) * t
-        const float px = a0.x + (b0.x - a0.x) * t, py = a0.y + (b0.y - a0.y) * t;
-        r.uv[2 * k] = a0.z + (b0.z - a0.z) * t;
-        r.uv[2 * k + 1] = a0.w + (b0.w - a0.w) * t;
-        r.rrel[k] = a1.x + (b1.x - a1.x) * t;
-        r.refl[k] = a1.y + (b1.y - a1.y) * t;
-        r.inten[k] = a1.z + (b1.z - a1.z) * t;
-        const float sx = px * S, sy = py * S;
-        finite = finite && fabsf(sx) < 16383.0f && fabsf(sy) < 16383.0f;
-        r.q[2 * k] = cvt_rz_sat(sx);
-        r.q[2 * k + 1] = cvt_rz_sat(sy);
-    }
-    const int* q = r.q;
-    edge_coeffs(q[0], q[1], q[2], q[3], r.ec + 0);
-    edge_coeffs(q[2], q[3], q[4], q[5], r.ec + 3);
-    edge_coeffs(q[4], q[5], q[6], q[7], r.ec + 6);
-    edge_coeffs(q[6], q[7], q[0], q[1], r.ec + 9);
-    edge_coeffs(q[4], q[5], q[0], q[1], r.ec + 12);
-    r.bb[0] = min(min(q[0], q[2]), min(q[4], q[6]));
-    r.bb[1] = max(max(q[0], q[2]), max(q[4], q[6]));
-    r.bb[2] = min(min(q[1], q[3]), min(q[5], q[7]));
-    r.bb[3] = max(max(q[1], q[3]), max(q[5], q[7]));
-    int flags = (finite && p.safe_screen) ? 1 : 0;
-    if (edge_i(q[0], q[1], q[2], q[3], q[4], q[5]) == 0 && edge_i(q[0], q[1], q[4], q[5], q[6], q[7]) == 0)
-        flags |= 2;
-    r.flags = flags;
-    r.color = w * p.WS + i;
-}
-
-// Mean-value weights (compute_barycentric_quad, rasterizing.cl:95-148). The half-angle
-// tangents t_i = (r_i r_j - d_i) / a_i amplify rounding where a_i is small next to
-// r_i r_j (and where a_i is 0 the reference divides the rounding residue of r_i r_j - d_i
-// by 1e-3): there t_i is evaluated with the reference's exact FP32 operations (correctly
-// rounded square roots, products, difference and quotient, never fused). Everywhere else,
-// and for the well-conditioned divisions by r_i and by the weight sum, reciprocal and
-// reciprocal-square-root instructions give the same values within a few ulps.
-__device__ __forceinline__ void barycentric_fast(const int* q, int px, int py, float w[4]) {
+// Mean-value weights (compute_barycentric_quad, rasterizing.cl:95-148) at the integer
+// sample point (px, py). The coordinates s_i = q_i - p are exact floats; the products
+// a_i, d_i, |s_i|^2 are exact integers wherever |s| < 4096, so fused multiply-adds give
+// the reference's values there. Where a_i is 0 the reference divides the rounding residue
+// of r_i r_j - d_i by 1e-3: that tangent is evaluated with the reference's exact FP32
+// operations (correctly rounded square roots, product, difference, quotient). Elsewhere
+// the tangents and the divisions by r_i and by the weight sum use reciprocal and
+// reciprocal-square-root instructions (a few ulps).
+__device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float py, float w[4]) {
     float sx[4], sy[4], a[4], d[4], r2[4], r[4], ir[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        sx[i] = (float)wsub(q[2 * i], px);
-        sy[i] = (float)wsub(q[2 * i + 1], py);
+        sx[i] = rec.qf[2 * i] - px;
+        sy[i] = rec.qf[2 * i + 1] - py;
     }
     bool zero = false;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const int j = (i + 1) & 3;
-        a[i] = __fsub_rn(__fmul_rn(sx[i], sy[j]), __fmul_rn(sx[j], sy[i]));
-        d[i] = __fadd_rn(__fmul_rn(sx[i], sx[j]), __fmul_rn(sy[i], sy[j]));
-        r2[i] = __fadd_rn(__fmul_rn(sx[i], sx[i]), __fmul_rn(sy[i], sy[i]));
+        a[i] = sx[i] * sy[j] - sx[j] * sy[i];
+        d[i] = sx[i] * sx[j] + sy[i] * sy[j];
+        r2[i] = sx[i] * sx[i] + sy[i] * sy[i];
         zero = zero || r2[i] == 0.0f;
         ir[i] = rsqrtf(r2[i]);
         r[i] = r2[i] * ir[i];
@@ -219,7 +132,9 @@ __device__ __forceinline__ void barycentric_fast(const int* q, int px, int py, f
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const int j = (i + 1) & 3;
-        if (a[i] * a[i] < (1.0f / 4096.0f) * r2[i] * r2[j]) {
+        const bool exact = RF_RASTER_EXACT_SMALL_ANGLES ? a[i] * a[i] < (1.0f / 4096.0f) * r2[i] * r2[j]
+                                                        : a[i] == 0.0f;
+        if (exact) {
             const float ai = a[i] == 0.0f ? 1e-3f : a[i];
             t[i] = __fdiv_rn(__fsub_rn(__fmul_rn(__fsqrt_rn(r2[i]), __fsqrt_rn(r2[j])), d[i]), ai);
         } else {
@@ -233,21 +148,55 @@ __device__ __forceinline__ void barycentric_fast(const int* q, int px, int py, f
     for (int i = 0; i < 4; i++) w[i] *= inv;
 }
 
-// fragment_shader (rasterizing.cl:471-506) times the hit count; inv_scale = 1 / ghost_scale
+// Bilinear ghost sample (read_imagef LINEAR, CLAMP -> border 0, rasterizing.cl:483-485)
+// at texel coordinates (u, v) = uv * size - 0.5.
+__device__ __forceinline__ float ghost_sample(const float* __restrict__ tex, int w, int h, float u, float v) {
+    if (!(fabsf(u) < 1e9f) || !(fabsf(v) < 1e9f)) return 0.0f;  // non-finite or far outside
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const int i0 = (int)fu, j0 = (int)fv;
+    const bool i0_in = (unsigned)i0 < (unsigned)w, i1_in = (unsigned)(i0 + 1) < (unsigned)w;
+    const bool j0_in = (unsigned)j0 < (unsigned)h, j1_in = (unsigned)(j0 + 1) < (unsigned)h;
+    // load from clamped (always valid) addresses, then zero the texels outside the image
+    const int ia = min(max(i0, 0), w - 1), ib = min(max(i0 + 1, 0), w - 1);
+    const float* row0 = tex + (size_t)min(max(j0, 0), h - 1) * w;
+    const float* row1 = tex + (size_t)min(max(j0 + 1, 0), h - 1) * w;
+    const float t00 = (i0_in && j0_in) ? __ldg(row0 + ia) : 0.0f;
+    const float t10 = (i1_in && j0_in) ? __ldg(row0 + ib) : 0.0f;
+    const float t01 = (i0_in && j1_in) ? __ldg(row1 + ia) : 0.0f;
+    const float t11 = (i1_in && j1_in) ? __ldg(row1 + ib) : 0.0f;
+    return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
+}
+
+// fragment_shader (rasterizing.cl:471-506) times the hit count. The texture coordinate
+// ((uv / scale + 1) / 2) * size - 0.5 is evaluated as uv * tex_scale + tex_offset.
+struct FragmentConsts {
+    float tsx, tox, tsy, toy;  // texel coordinate scale and offset per axis
+};
 __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], const float* __restrict__ ghost,
-                                               const RasterParams& p, float inv_scale, int hits) {
-    float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
-    float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
-    u = (u * inv_scale + 1.0f) * 0.5f;
-    v = (v * inv_scale + 1.0f) * 0.5f;
-    const float gi = sample_linear(ghost, p.ghost_w, p.ghost_h, 1, 0, u, v, false);
+                                               const RasterParams& p, const FragmentConsts& fc, int hits) {
+    const float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
+    const float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
+    const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox, v * fc.tsy + fc.toy);
     const float rr = w[0] * r.rrel[0] + w[1] * r.rrel[1] + w[2] * r.rrel[2] + w[3] * r.rrel[3];
-    const float ri = smoothstepf(1.0f, 0.95f, rr);
+    // smoothstep(1, 0.95, rr) with the division by the constant (0.95 - 1) as a product
+    const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
+    const float ri = st * st * (3.0f - 2.0f * st);
     float ai = w[0] * r.inten[0] + w[1] * r.inten[1] + w[2] * r.inten[2] + w[3] * r.inten[3];
     float ci = w[0] * r.refl[0] + w[1] * r.refl[1] + w[2] * r.refl[2] + w[3] * r.refl[3];
     ai = fmaxf(ai, 0.0f);
     ci = fmaxf(ci, 0.0f);
     return gi * ri * ai * ci * (float)hits;
+}
+
+inline FragmentConsts fragment_consts(const RasterParams& p) {
+    FragmentConsts fc;
+    const double sx = 0.5 / p.ghost_scale * p.ghost_w, sy = 0.5 / p.ghost_scale * p.ghost_h;
+    fc.tsx = (float)sx;
+    fc.tsy = (float)sy;
+    fc.tox = (float)(0.5 * p.ghost_w - 0.5);
+    fc.toy = (float)(0.5 * p.ghost_h - 0.5);
+    return fc;
 }
 
 // Corner k of entry `entry` at the pair's two wavelengths: vertex words a0, a1 (first
@@ -280,6 +229,8 @@ __device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t
     r.inten[k] = c.a1.z + (c.b1.z - c.a1.z) * t;
     r.q[2 * k] = cvt_rz_sat(px * (float)S);
     r.q[2 * k + 1] = cvt_rz_sat(py * (float)S);
+    r.qf[2 * k] = (float)r.q[2 * k];
+    r.qf[2 * k + 1] = (float)r.q[2 * k + 1];
 }
 // edges, bounds and flags of a record whose corners are stored
 __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int i, Rec& r) {
@@ -311,12 +262,12 @@ __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int 
 constexpr int kTile = 32;
 constexpr int kThreads = 256;
 
-__global__ void __launch_bounds__(kThreads, 3) k_raster(const float4* __restrict__ vtx,
+__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const float4* __restrict__ vtx,
                                                        const uint32_t* __restrict__ tile_offsets,
                                                        const uint32_t* __restrict__ tile_entries,
                                                        const float* __restrict__ ghost,
                                                        const float* __restrict__ spectrum, RasterParams p,
-                                                       float4* __restrict__ image) {
+                                                       FragmentConsts fcs, float4* __restrict__ image) {
     extern __shared__ float4 smem4[];
     Rec* recs = (Rec*)smem4;
     float* xyz = (float*)(recs + kBatchRecords);  // [maxW * WS][3]
@@ -348,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_raster(const float4* __restrict
     }
 
     const int S = p.S;
-    const float inv_scale = 1.0f / p.ghost_scale;
+    const FragmentConsts fc = fcs;
     // per-thread accumulators of the four pixels, [k * 3 + channel][thread]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
@@ -428,8 +379,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_raster(const float4* __restrict
                     for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
                     if (hits == 0) continue;
                     float wt[4];
-                    barycentric_fast(r.q, sx0 + S / 2, sy0 + S / 2, wt);
-                    const float f = fragment_fast(r, wt, ghost, p, inv_scale, hits);
+                    barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
+                    const float f = fragment_fast(r, wt, ghost, p, fc, hits);
                     if (p.W > 1) {
                         const float* c = xyz + 3 * r.color;
                         r0 += c[0] * f;
@@ -467,7 +418,7 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
                                                       const unsigned long long* __restrict__ masks, int batch_count,
                                                       int B, long long prim_total, const float* __restrict__ ghost,
                                                       const float* __restrict__ spectrum, RasterParams p,
-                                                      float4* __restrict__ image) {
+                                                      FragmentConsts fc, float4* __restrict__ image) {
     const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
     if (x >= p.width || y >= p.height) return;
     const int bdx = (p.width + B - 1) / B;
@@ -508,6 +459,8 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
                         r.inten[c] = a1.z + (b1.z - a1.z) * sub_pos;
                         r.q[2 * c] = cvt_rz_sat(px * (float)S);
                         r.q[2 * c + 1] = cvt_rz_sat(py * (float)S);
+                        r.qf[2 * c] = (float)r.q[2 * c];
+                        r.qf[2 * c + 1] = (float)r.q[2 * c + 1];
                     }
                     const int* qq = r.q;
                     edge_coeffs(qq[0], qq[1], qq[2], qq[3], r.ec + 0);
@@ -523,8 +476,8 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
                     float f = 0.0f;
                     if (hits > 0) {
                         float wt[4];
-                        barycentric_fast(r.q, sx0 + S / 2, sy0 + S / 2, wt);
-                        f += fragment_fast(r, wt, ghost, p, 1.0f / p.ghost_scale, hits);
+                        barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
+                        f += fragment_fast(r, wt, ghost, p, fc, hits);
                     }
                     if (p.W > 1) {
                         for (int c = 0; c < 3; c++)
@@ -578,7 +531,7 @@ int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t
     if (smem > 48 * 1024)
         RF_TRY(cuda_status(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
     k_raster<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum, p,
-                                                (float4*)image);
+                                                fragment_consts(p), (float4*)image);
     return launch_status();
 }
 
@@ -608,6 +561,6 @@ extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
     k_raster_masks<<<grid, 256, 0, (cudaStream_t)stream>>>((const float4*)vertexes, (const unsigned long long*)masks,
                                                            batch_count, args->bin_size, prim_total, ghost, spectrum,
-                                                           p, (float4*)image);
+                                                           p, fragment_consts(p), (float4*)image);
     return launch_status();
 }
