@@ -34,10 +34,13 @@ namespace {
 // requested from the register allocator, and where the half-angle tangents use the
 // reference's exact FP32 operations (1: small angles, 0: only a_i == 0).
 #ifndef RF_RASTER_BATCH
-#define RF_RASTER_BATCH 128
+#define RF_RASTER_BATCH 64
 #endif
 #ifndef RF_RASTER_MIN_BLOCKS
 #define RF_RASTER_MIN_BLOCKS 3
+#endif
+#ifndef RF_RASTER_CLASSIFY
+#define RF_RASTER_CLASSIFY 1
 #endif
 #ifndef RF_RASTER_EXACT_SMALL_ANGLES
 #define RF_RASTER_EXACT_SMALL_ANGLES 0
@@ -91,6 +94,28 @@ __device__ __forceinline__ bool inside(const Rec& r, int px, int py) {
     const bool front = (w20 && w01 && w12 && (w23 || w30)) || (!w20 && w23 && w30 && (w01 || w12));
     const bool back = (!w20 && !w01 && !w12 && (!w23 || !w30)) || (w20 && !w23 && !w30 && (!w01 || !w12));
     return front || back;
+}
+
+// Coverage of the sample rectangle [x0, x1] x [y0, y1] by a record whose coordinates
+// keep every edge value exact (flags & 1): each edge value is linear in the sample, so
+// its sign is constant over the rectangle when its minimum and maximum there (over the
+// corners) agree, and then inside() is constant too. Returns 0 (no sample inside),
+// 2 (every sample inside) or 1 (mixed or undecided).
+__device__ __forceinline__ int rect_coverage(const Rec& r, int x0, int x1, int y0, int y1) {
+    bool w[5];
+#pragma unroll
+    for (int e = 0; e < 5; e++) {
+        const int A = r.ec[3 * e], B = r.ec[3 * e + 1], C = r.ec[3 * e + 2];
+        const int ay0 = A * y0, ay1 = A * y1, bx0 = B * x0, bx1 = B * x1;
+        const int lo = C + min(ay0, ay1) + min(bx0, bx1);
+        const int hi = C + max(ay0, ay1) + max(bx0, bx1);
+        if (lo < 0 && hi >= 0) return 1;
+        w[e] = lo >= 0;
+    }
+    const bool w01 = w[0], w12 = w[1], w23 = w[2], w30 = w[3], w20 = w[4];
+    const bool front = (w20 && w01 && w12 && (w23 || w30)) || (!w20 && w23 && w30 && (w01 || w12));
+    const bool back = (!w20 && !w01 && !w12 && (!w23 || !w30)) || (w20 && !w23 && !w30 && (!w01 || !w12));
+    return (front || back) ? 2 : 0;
 }
 
 // Mean-value weights (compute_barycentric_quad, rasterizing.cl:95-148) at the integer
@@ -310,10 +335,10 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
     // thread j loads corner j % 4 of entry j / 4 of the batch; the next batch is
     // prefetched into registers while the current one is shaded
     const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
-    CornerLoad next[kBatchRecords / 64];
-    bool have_next[kBatchRecords / 64];
+    CornerLoad next[(kBatchRecords + 63) / 64];
+    bool have_next[(kBatchRecords + 63) / 64];
 #pragma unroll
-    for (int h = 0; h < kBatchRecords / 64; h++) {
+    for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
         const int e = my_entry + 64 * h;
         have_next[h] = e < per_batch && begin + e < end;
         if (have_next[h]) load_corner(vtx, tile_entries[begin + e], my_corner, p, next[h]);
@@ -323,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
         const int n_rec = n_entries * p.WS;
         __syncthreads();  // the previous batch is shaded
 #pragma unroll
-        for (int h = 0; h < kBatchRecords / 64; h++) {
+        for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
             const int e = my_entry + 64 * h;
             if (have_next[h])
                 for (int i = 0; i < p.WS; i++) store_corner(next[h], my_corner, blend[i], S, recs[e * p.WS + i]);
@@ -344,21 +369,30 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
             const bool in_image = px < p.width && py < p.height;
             const int sx0 = px * S, sy0 = py * S;
-            // which records can touch this 8 x 4 block: lanes test 32 records at a time
-            unsigned sel[kBatchRecords / 32];
+            // which records can touch this 8 x 4 block, and which cover all of it: lanes
+            // test 32 records at a time
+            unsigned sel[kBatchRecords / 32], whole[kBatchRecords / 32];
 #pragma unroll
             for (int m = 0; m < kBatchRecords / 32; m++) {
                 const int j = m * 32 + lane;
-                bool take = false;
+                bool take = false, all = false;
                 if (j < n_rec) {
                     const Rec& r = recs[j];
                     const int flags = r.flags;
                     if (!(flags & 2)) {  // both triangles collinear: intersect_quad rejects all
                         const int4 bb = *reinterpret_cast<const int4*>(r.bb);
                         take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);
+#if RF_RASTER_CLASSIFY
+                        if (take && (flags & 1)) {
+                            const int cov = rect_coverage(r, bx0, bx1, by0, by1);
+                            take = cov != 0;
+                            all = cov == 2;
+                        }
+#endif
                     }
                 }
                 sel[m] = __ballot_sync(0xffffffffu, take);
+                whole[m] = __ballot_sync(0xffffffffu, all);
             }
             float r0 = acc[(3 * k) * kThreads + threadIdx.x];
             float r1 = acc[(3 * k + 1) * kThreads + threadIdx.x];
@@ -367,17 +401,21 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             for (int m = 0; m < kBatchRecords / 32; m++) {
                 unsigned bits = sel[m];
                 while (bits) {  // in increasing record order: the reference's summation order
-                    const int j = m * 32 + __ffs(bits) - 1;
+                    const int b = __ffs(bits) - 1;
+                    const int j = m * 32 + b;
                     bits &= bits - 1;
                     const Rec& r = recs[j];
                     if (!in_image) continue;
-                    if (r.flags & 1) {
-                        const int4 bb = *reinterpret_cast<const int4*>(r.bb);
-                        if (sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w) continue;
+                    int hits = S;
+                    if (!((whole[m] >> b) & 1u)) {
+                        if (r.flags & 1) {
+                            const int4 bb = *reinterpret_cast<const int4*>(r.bb);
+                            if (sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w) continue;
+                        }
+                        hits = 0;
+                        for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
+                        if (hits == 0) continue;
                     }
-                    int hits = 0;
-                    for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
-                    if (hits == 0) continue;
                     float wt[4];
                     barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
                     const float f = fragment_fast(r, wt, ghost, p, fc, hits);
