@@ -46,7 +46,23 @@ def parse_args():
     ap.add_argument('--workload', default=WORKLOAD)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    # reductions of the workload for profiler captures (recorded in the line's config)
+    ap.add_argument('--image', type=int, default=0, help='square image size override')
+    ap.add_argument('--ghosts', type=int, default=0, help='keep only the first N ghosts')
     return ap.parse_args()
+
+
+def make_workload(args):
+    from realflare_gb300 import synthetic
+    from realflare_gb300.data import QSize
+
+    w = synthetic.workload(args.workload)
+    lens = w.project.flare.lens
+    if args.image > 0:
+        w.project.render.resolution = QSize(args.image, args.image)
+    if args.ghosts > 0:
+        lens.ghost_paths = lens.ghost_paths[:args.ghosts]
+    return w
 
 
 def dist_init():
@@ -439,11 +455,9 @@ def raster_traffic_per_entry() -> float | None:
 
 
 def run_reference(args, rank, world) -> None:
-    from realflare_gb300 import synthetic
-
     if rank != 0:
         return
-    w = synthetic.workload(args.workload)
+    w = make_workload(args)
     cpu = CpuBaseline(w)
     stages, times = None, []
     for i in range(args.warmup + args.steps):
@@ -475,10 +489,9 @@ def main() -> None:
         return
     import torch
 
-    from realflare_gb300 import synthetic
     from realflare_gb300._abi import lib
 
-    w = synthetic.workload(args.workload)
+    w = make_workload(args)
     frame = GpuFrame(w)
     for _ in range(max(args.warmup, 3)):
         frame.step()

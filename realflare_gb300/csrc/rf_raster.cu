@@ -42,6 +42,9 @@ namespace {
 #ifndef RF_RASTER_CLASSIFY
 #define RF_RASTER_CLASSIFY 1
 #endif
+#ifndef RF_RASTER_DYNAMIC
+#define RF_RASTER_DYNAMIC 1
+#endif
 #ifndef RF_RASTER_EXACT_SMALL_ANGLES
 #define RF_RASTER_EXACT_SMALL_ANGLES 0
 #endif
@@ -294,6 +297,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                                                        const float* __restrict__ spectrum, RasterParams p,
                                                        FragmentConsts fcs, float4* __restrict__ image) {
     extern __shared__ float4 smem4[];
+    __shared__ int next_block;  // blocks of the current batch handed out so far
     Rec* recs = (Rec*)smem4;
     float* xyz = (float*)(recs + kBatchRecords);  // [maxW * WS][3]
     float* blend = xyz + 3 * p.maxW * p.WS;       // [WS]
@@ -325,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
 
     const int S = p.S;
     const FragmentConsts fc = fcs;
-    // per-thread accumulators of the four pixels, [k * 3 + channel][thread]
+    // accumulators of the 32 pixel blocks, [block * 3 + channel][lane]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
     for (int c = 0; c < 12; c++) acc[c * kThreads + threadIdx.x] = 0.0f;
@@ -355,15 +359,27 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             have_next[h] = e < per_batch && base + per_batch + e < end;
             if (have_next[h]) load_corner(vtx, tile_entries[base + per_batch + e], my_corner, p, next[h]);
         }
+        if (threadIdx.x == 0) next_block = 0;
         __syncthreads();
         for (int j = threadIdx.x; j < n_rec; j += kThreads) {
             const uint32_t entry = tile_entries[base + j / p.WS];
             finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
         }
         __syncthreads();
+        // Warps take the tile's 8 x 4 blocks one at a time (blocks differ widely in work);
+        // a block is shaded by one warp per batch, batches in order, so every pixel still
+        // adds its records in increasing order.
 #pragma unroll 1
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0;; k++) {
+#if RF_RASTER_DYNAMIC
+            int blk = 0;
+            if (lane == 0) blk = atomicAdd(&next_block, 1);
+            blk = __shfl_sync(0xffffffffu, blk, 0);
+            if (blk >= 32) break;
+#else
+            if (k == 4) break;
             const int blk = warp + 8 * k;
+#endif
             const int x0 = tx * kTile + (blk & 3) * 8, y0 = ty * kTile + (blk >> 2) * 4;
             const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
@@ -394,9 +410,9 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                 sel[m] = __ballot_sync(0xffffffffu, take);
                 whole[m] = __ballot_sync(0xffffffffu, all);
             }
-            float r0 = acc[(3 * k) * kThreads + threadIdx.x];
-            float r1 = acc[(3 * k + 1) * kThreads + threadIdx.x];
-            float r2 = acc[(3 * k + 2) * kThreads + threadIdx.x];
+            float r0 = acc[(3 * blk) * 32 + lane];
+            float r1 = acc[(3 * blk + 1) * 32 + lane];
+            float r2 = acc[(3 * blk + 2) * 32 + lane];
 #pragma unroll
             for (int m = 0; m < kBatchRecords / 32; m++) {
                 unsigned bits = sel[m];
@@ -431,20 +447,21 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                     }
                 }
             }
-            acc[(3 * k) * kThreads + threadIdx.x] = r0;
-            acc[(3 * k + 1) * kThreads + threadIdx.x] = r1;
-            acc[(3 * k + 2) * kThreads + threadIdx.x] = r2;
+            acc[(3 * blk) * 32 + lane] = r0;
+            acc[(3 * blk + 1) * 32 + lane] = r1;
+            acc[(3 * blk + 2) * 32 + lane] = r2;
         }
     }
 
+    __syncthreads();  // every block's last batch is shaded
     const float scale = p.intensity / (float)(p.W * p.S * p.WS);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const int blk = warp + 8 * k;
         const int px = tx * kTile + (blk & 3) * 8 + (lane & 7), py = ty * kTile + (blk >> 2) * 4 + (lane >> 3);
         if (px >= p.width || py >= p.height) continue;
-        const float c0 = acc[(3 * k) * kThreads + threadIdx.x], c1 = acc[(3 * k + 1) * kThreads + threadIdx.x],
-                    c2 = acc[(3 * k + 2) * kThreads + threadIdx.x];
+        const float c0 = acc[(3 * blk) * 32 + lane], c1 = acc[(3 * blk + 1) * 32 + lane],
+                    c2 = acc[(3 * blk + 2) * 32 + lane];
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c0 > 0.0f || c1 > 0.0f || c2 > 0.0f) out = xyz_to_ap1(c0 * scale, c1 * scale, c2 * scale);
         image[(size_t)(p.height - (py + 1)) * p.width + px] = out;
