@@ -42,9 +42,6 @@ namespace {
 #ifndef RF_RASTER_CLASSIFY
 #define RF_RASTER_CLASSIFY 1
 #endif
-#ifndef RF_RASTER_DYNAMIC
-#define RF_RASTER_DYNAMIC 1
-#endif
 #ifndef RF_RASTER_EXACT_SMALL_ANGLES
 #define RF_RASTER_EXACT_SMALL_ANGLES 0
 #endif
@@ -130,43 +127,55 @@ __device__ __forceinline__ int rect_coverage(const Rec& r, int x0, int x1, int y
 // the tangents and the divisions by r_i and by the weight sum use reciprocal and
 // reciprocal-square-root instructions (a few ulps).
 __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float py, float w[4]) {
-    float sx[4], sy[4], a[4], d[4], r2[4], r[4], ir[4];
+    float sx[4], sy[4], a[4], d[4], r2[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         sx[i] = rec.qf[2 * i] - px;
         sy[i] = rec.qf[2 * i + 1] - py;
     }
-    bool zero = false;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const int j = (i + 1) & 3;
         a[i] = sx[i] * sy[j] - sx[j] * sy[i];
         d[i] = sx[i] * sx[j] + sy[i] * sy[j];
         r2[i] = sx[i] * sx[i] + sy[i] * sy[i];
-        zero = zero || r2[i] == 0.0f;
+    }
+    // a_i and r2_i are integers (differences and sums of products of integers), so a product
+    // of the four is 0 exactly when one of them is 0, and otherwise at least 1 and finite
+    const bool rare = (a[0] * a[1]) * (a[2] * a[3]) == 0.0f || (r2[0] * r2[1]) * (r2[2] * r2[3]) == 0.0f;
+    float ir[4], r[4], t[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
         ir[i] = rsqrtf(r2[i]);
         r[i] = r2[i] * ir[i];
     }
-    if (zero) {  // a vertex on the sample point: one-hot on the first such vertex
-        int k = 0;
+    if (!rare) {
 #pragma unroll
-        for (int i = 3; i >= 0; i--)
-            if (sx[i] == 0.0f && sy[i] == 0.0f) k = i;
+        for (int i = 0; i < 4; i++) t[i] = (r[i] * r[(i + 1) & 3] - d[i]) * __fdividef(1.0f, a[i]);
+    } else {
+        bool zero = false;
 #pragma unroll
-        for (int i = 0; i < 4; i++) w[i] = i == k ? 1.0f : 0.0f;
-        return;
-    }
-    float t[4];
+        for (int i = 0; i < 4; i++) zero = zero || r2[i] == 0.0f;
+        if (zero) {  // a vertex on the sample point: one-hot on the first such vertex
+            int k = 0;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int j = (i + 1) & 3;
-        const bool exact = RF_RASTER_EXACT_SMALL_ANGLES ? a[i] * a[i] < (1.0f / 4096.0f) * r2[i] * r2[j]
-                                                        : a[i] == 0.0f;
-        if (exact) {
-            const float ai = a[i] == 0.0f ? 1e-3f : a[i];
-            t[i] = __fdiv_rn(__fsub_rn(__fmul_rn(__fsqrt_rn(r2[i]), __fsqrt_rn(r2[j])), d[i]), ai);
-        } else {
-            t[i] = (r[i] * r[j] - d[i]) * __fdividef(1.0f, a[i]);
+            for (int i = 3; i >= 0; i--)
+                if (sx[i] == 0.0f && sy[i] == 0.0f) k = i;
+#pragma unroll
+            for (int i = 0; i < 4; i++) w[i] = i == k ? 1.0f : 0.0f;
+            return;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int j = (i + 1) & 3;
+            const bool exact = RF_RASTER_EXACT_SMALL_ANGLES ? a[i] * a[i] < (1.0f / 4096.0f) * r2[i] * r2[j]
+                                                            : a[i] == 0.0f;
+            if (exact) {
+                const float ai = a[i] == 0.0f ? 1e-3f : a[i];
+                t[i] = __fdiv_rn(__fsub_rn(__fmul_rn(__fsqrt_rn(r2[i]), __fsqrt_rn(r2[j])), d[i]), ai);
+            } else {
+                t[i] = (r[i] * r[j] - d[i]) * __fdividef(1.0f, a[i]);
+            }
         }
     }
 #pragma unroll
@@ -297,9 +306,9 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                                                        const float* __restrict__ spectrum, RasterParams p,
                                                        FragmentConsts fcs, float4* __restrict__ image) {
     extern __shared__ float4 smem4[];
-    __shared__ int next_block;  // blocks of the current batch handed out so far
-    Rec* recs = (Rec*)smem4;
-    float* xyz = (float*)(recs + kBatchRecords);  // [maxW * WS][3]
+    __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
+    Rec* recbuf = (Rec*)smem4;     // two batches of records
+    float* xyz = (float*)(recbuf + 2 * kBatchRecords);  // [maxW * WS][3]
     float* blend = xyz + 3 * p.maxW * p.WS;       // [WS]
 
     const int tile = blockIdx.x;
@@ -336,50 +345,65 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
 
     const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
     const int per_batch = kBatchRecords / p.WS;  // entries per batch (WS <= kBatchRecords)
-    // thread j loads corner j % 4 of entry j / 4 of the batch; the next batch is
-    // prefetched into registers while the current one is shaded
+    // Batches of records are double-buffered: while warps shade batch t from one buffer,
+    // warps that are done build batch t + 1 in the other, one barrier per batch. Thread j
+    // loads corner j % 4 of entry j / 4 (the four corners of an entry sit in one warp), one
+    // batch ahead, into registers.
     const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
-    CornerLoad next[(kBatchRecords + 63) / 64];
-    bool have_next[(kBatchRecords + 63) / 64];
+    constexpr int kLoads = (kBatchRecords + 63) / 64;
+    CornerLoad next[kLoads];
+    int next_w[kLoads];
+    bool have_next[kLoads];
+    auto prefetch = [&](uint32_t first) {
 #pragma unroll
-    for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
-        const int e = my_entry + 64 * h;
-        have_next[h] = e < per_batch && begin + e < end;
-        if (have_next[h]) load_corner(vtx, tile_entries[begin + e], my_corner, p, next[h]);
-    }
-    for (uint32_t base = begin; base < end; base += per_batch) {
-        const int n_entries = (int)min((uint32_t)per_batch, end - base);
-        const int n_rec = n_entries * p.WS;
-        __syncthreads();  // the previous batch is shaded
+        for (int h = 0; h < kLoads; h++) {
+            const int e = my_entry + 64 * h;
+            have_next[h] = e < per_batch && first + e < end;
+            if (have_next[h]) {
+                const uint32_t entry = tile_entries[first + e];
+                next_w[h] = (int)(entry % p.maxW);
+                load_corner(vtx, entry, my_corner, p, next[h]);
+            }
+        }
+    };
+    // records of the prefetched batch into dst, then prefetch the batch after it
+    auto build = [&](Rec* dst, uint32_t first) {
 #pragma unroll
-        for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
+        for (int h = 0; h < kLoads; h++) {
             const int e = my_entry + 64 * h;
             if (have_next[h])
-                for (int i = 0; i < p.WS; i++) store_corner(next[h], my_corner, blend[i], S, recs[e * p.WS + i]);
-            have_next[h] = e < per_batch && base + per_batch + e < end;
-            if (have_next[h]) load_corner(vtx, tile_entries[base + per_batch + e], my_corner, p, next[h]);
+                for (int i = 0; i < p.WS; i++) store_corner(next[h], my_corner, blend[i], S, dst[e * p.WS + i]);
         }
-        if (threadIdx.x == 0) next_block = 0;
-        __syncthreads();
-        for (int j = threadIdx.x; j < n_rec; j += kThreads) {
-            const uint32_t entry = tile_entries[base + j / p.WS];
-            finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
+        __syncwarp();  // the four corners of each record are stored
+#pragma unroll
+        for (int h = 0; h < kLoads; h++) {
+            const int e = my_entry + 64 * h;
+            if (have_next[h])
+                for (int i = my_corner; i < p.WS; i += 4) finish_record(p, next_w[h], i, dst[e * p.WS + i]);
         }
-        __syncthreads();
+        prefetch(first + per_batch);
+    };
+    if (threadIdx.x == 0) {
+        next_block[0] = 0;
+        next_block[1] = 0;
+    }
+    prefetch(begin);
+    __syncthreads();  // blend weights and colours are set
+    if (begin < end) build(recbuf, begin);
+    __syncthreads();
+    int cur = 0;
+    for (uint32_t base = begin; base < end; base += per_batch, cur ^= 1) {
+        const int n_rec = (int)min((uint32_t)per_batch, end - base) * p.WS;
+        const Rec* recs = recbuf + cur * kBatchRecords;
         // Warps take the tile's 8 x 4 blocks one at a time (blocks differ widely in work);
         // a block is shaded by one warp per batch, batches in order, so every pixel still
         // adds its records in increasing order.
 #pragma unroll 1
-        for (int k = 0;; k++) {
-#if RF_RASTER_DYNAMIC
+        for (;;) {
             int blk = 0;
-            if (lane == 0) blk = atomicAdd(&next_block, 1);
+            if (lane == 0) blk = atomicAdd(&next_block[cur], 1);
             blk = __shfl_sync(0xffffffffu, blk, 0);
             if (blk >= 32) break;
-#else
-            if (k == 4) break;
-            const int blk = warp + 8 * k;
-#endif
             const int x0 = tx * kTile + (blk & 3) * 8, y0 = ty * kTile + (blk >> 2) * 4;
             const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
@@ -419,11 +443,12 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                 while (bits) {  // in increasing record order: the reference's summation order
                     const int b = __ffs(bits) - 1;
                     const int j = m * 32 + b;
+                    const bool is_whole = (whole[m] >> b) & 1u;
                     bits &= bits - 1;
                     const Rec& r = recs[j];
                     if (!in_image) continue;
                     int hits = S;
-                    if (!((whole[m] >> b) & 1u)) {
+                    if (!is_whole) {
                         if (r.flags & 1) {
                             const int4 bb = *reinterpret_cast<const int4*>(r.bb);
                             if (sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w) continue;
@@ -451,6 +476,10 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             acc[(3 * blk + 1) * 32 + lane] = r1;
             acc[(3 * blk + 2) * 32 + lane] = r2;
         }
+        if (base + per_batch < end) build(recbuf + (cur ^ 1) * kBatchRecords, base + per_batch);
+        // the other counter was last used by the previous batch, behind the last barrier
+        if (threadIdx.x == 0) next_block[cur ^ 1] = 0;
+        __syncthreads();
     }
 
     __syncthreads();  // every block's last batch is shaded
@@ -581,7 +610,7 @@ int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t
     p.T = kTile;
     p.ntx = (p.width + kTile - 1) / kTile;
     const int nty = (p.height + kTile - 1) / kTile;
-    const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
+    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
                         sizeof(float) * 12 * kThreads;
     if (smem > 48 * 1024)
         RF_TRY(cuda_status(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
