@@ -49,6 +49,8 @@ def parse_args():
     # reductions of the workload for profiler captures (recorded in the line's config)
     ap.add_argument('--image', type=int, default=0, help='square image size override')
     ap.add_argument('--ghosts', type=int, default=0, help='keep only the first N ghosts')
+    ap.add_argument('--raster-stats', action='store_true',
+                    help='count k_raster work (statistics build of the library) instead of timing')
     return ap.parse_args()
 
 
@@ -444,14 +446,15 @@ def load_peaks() -> tuple:
         return 6800.0, 'fallback'
 
 
-def raster_traffic_per_entry() -> float | None:
-    """DRAM bytes per tile entry of k_raster from the committed ncu summary."""
-    path = os.path.join(ROOT, 'profiles', 'k_raster_traffic.json')
+def raster_profile() -> dict:
+    """k_raster figures of the production frame from the committed ncu summary
+    (DRAM bytes of one launch, tile entries and fragments of that launch)."""
+    path = os.path.join(ROOT, 'profiles', 'k_raster_production-24.json')
     try:
         with open(path) as f:
-            return float(json.load(f)['dram_bytes_per_entry'])
-    except (OSError, KeyError, ValueError):
-        return None
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def run_reference(args, rank, world) -> None:
@@ -486,6 +489,9 @@ def main() -> None:
     rank, world = dist_init()
     if args.impl == 'reference':
         run_reference(args, rank, world)
+        return
+    if args.raster_stats:
+        run_raster_stats(args)
         return
     import torch
 
@@ -529,14 +535,20 @@ def main() -> None:
     h, wd = frame.flare.shape[:2]
     alg_bytes = entries * (4 + 4 * 64) + h * wd * 16
     achieved = alg_bytes / raster_s / 1e9
-    tpe = raster_traffic_per_entry()
+    prof = raster_profile()
+    traffic = fragments = None
+    if prof.get('workload') == args.workload and prof.get('tile_entries') == entries:
+        # the summary was taken on this very launch (same workload, same tile entries)
+        traffic = prof['dram_bytes']
+        fragments = prof['fragments']
     roofline = {
         'kernel': 'k_raster', 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
         'frac': achieved / peak, 'peak_source': f'{peak_kind} hbm_gbs',
-        'traffic': tpe * entries if tpe else None,
+        'traffic': traffic,
         'algorithmic_bytes': alg_bytes,
-        'note': ('compute/issue-bound per-fragment shading (about 21 G quad-pixel fragments per frame); '
-                 'the HBM fraction is reported per the contract'),
+        'fragments_per_s': fragments / raster_s if fragments else None,
+        'note': ('issue-bound per-fragment shading (mean-value weights, bilinear ghost lookup per covered '
+                 'pixel x record); the vertex reads hit L2, so DRAM traffic is far below the algorithmic bytes'),
     }
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -552,7 +564,9 @@ def main() -> None:
             'config': {
                 'workload': args.workload, 'image': f'{wd}x{h}', 'ghosts': frame.P, 'wavelengths': frame.W,
                 'grid': frame.G, 'rays_per_frame': frame.n_rays, 'starburst_aperture': '512x512',
-                'parallelism': f'replicas{world}', 'l2': 'per-frame working set (rays 1.7 GB, vertices 2.3 GB) > L2',
+                'parallelism': f'replicas{world}',
+                'l2': f'per-frame working set (rays {frame.rays.numel() * 4 / 1e9:.2f} GB, tile entries '
+                      f'{entries * 4 / 1e9:.2f} GB) > L2 (129 MB): no flush needed',
             },
             'rays_per_s': frame.n_rays / (last['trace'] / 1e3) * world,
             'stage_ms': {k: round(v, 3) for k, v in last.items()},
@@ -568,6 +582,46 @@ def main() -> None:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_raster_stats(args) -> None:
+    """One frame with the product library, then its raster pass again through the statistics
+    build, which counts record iterations per 8 x 4 block and fragments (covered pixel x
+    record pairs)."""
+    import ctypes
+
+    import torch
+
+    from realflare_gb300 import build as rf_build
+    from realflare_gb300._abi import SIGNATURES
+
+    frame = GpuFrame(make_workload(args))
+    frame.step()
+    torch.cuda.synchronize()
+    S = ctypes.CDLL(rf_build.build(stats=True))
+    S.rf_raster.argtypes = SIGNATURES['rf_raster']
+    S.rf_raster.restype = ctypes.c_int
+    S.rf_raster_stats.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
+    S.rf_raster_stats.restype = ctypes.c_int
+    out = (ctypes.c_ulonglong * 5)()
+    assert S.rf_raster_stats(out) == 0
+    r = frame.raster
+    st = S.rf_raster(r._buffers['vertexes'].data_ptr(), r._buffers['tile_offsets'].data_ptr(),
+                     r._buffers['tile_entries'].data_ptr(), frame.ghost.data_ptr(), frame.spectrum_tex.data_ptr(),
+                     ctypes.byref(frame.ra), frame.flare.data_ptr(), frame.sh)
+    torch.cuda.synchronize()
+    assert st == 0, st
+    assert S.rf_raster_stats(out) == 0
+    it, whole, frag, frag_whole, blocks = (int(v) for v in out)
+    h, wd = frame.flare.shape[:2]
+    print(json.dumps({
+        'raster_stats': {
+            'tile_entries': frame.entries, 'block_visits': blocks, 'record_iterations': it,
+            'whole_block_record_iterations': whole, 'fragments': frag, 'fragments_in_whole_blocks': frag_whole,
+            'fragments_per_pixel': frag / (h * wd), 'lane_efficiency': frag / max(1, 32 * it),
+        },
+        'config': {'workload': args.workload, 'image': f'{wd}x{h}', 'ghosts': frame.P},
+    }), flush=True)
 
 
 def run_e2e(w, args) -> dict:

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'librealflare_gb300.so')
+STATS_LIB = os.path.join(HERE, 'librealflare_gb300_stats.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 UNITS = {
@@ -47,18 +48,25 @@ def _stale(target: str, deps: list) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, stats: bool = False) -> str:
+    """Build the library; ``stats`` builds ``librealflare_gb300_stats.so`` instead, whose
+    k_raster also counts its record iterations and fragments (``rf_raster_stats``)."""
+    build_dir = os.path.join(BUILD, 'stats') if stats else BUILD
+    lib = STATS_LIB if stats else LIB
+    units = dict(UNITS)
+    if stats:
+        units['rf_raster.cu'] = units['rf_raster.cu'] + ['-DRF_RASTER_STATS=1']
+    os.makedirs(build_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith('.cuh')]
     headers.append(os.path.join(HERE, '..', 'include', 'realflare_gb300.h'))
-    flags_file = os.path.join(BUILD, 'flags.txt')
-    flag_sig = repr(sorted(UNITS.items()))
+    flags_file = os.path.join(build_dir, 'flags.txt')
+    flag_sig = repr(sorted(units.items()))
     if not os.path.exists(flags_file) or open(flags_file).read() != flag_sig:
         force = True
     objs, procs = [], []
-    for unit, extra in UNITS.items():
+    for unit, extra in units.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(BUILD, unit.replace('.cu', '.o'))
+        obj = os.path.join(build_dir, unit.replace('.cu', '.o'))
         objs.append(obj)
         if not force and not _stale(obj, [src] + headers):
             continue
@@ -76,14 +84,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
             failed.append(unit)
     if failed:
         raise RuntimeError(f'nvcc failed for {failed}')
-    if force or procs or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, '-shared', '-o', LIB + '.tmp', *objs, '-lcudart']
+    if force or procs or _stale(lib, objs):
+        cmd = [nvcc(), *ARCH, '-shared', '-o', lib + '.tmp', *objs, '-lcudart']
         subprocess.check_call(cmd)
-        os.replace(LIB + '.tmp', LIB)
+        os.replace(lib + '.tmp', lib)
     with open(flags_file, 'w') as f:
         f.write(flag_sig)
-    return LIB
+    return lib
 
 
 if __name__ == '__main__':
-    print(build(force='--force' in sys.argv, verbose='-v' in sys.argv))
+    print(build(force='--force' in sys.argv, verbose='-v' in sys.argv, stats='--stats' in sys.argv))

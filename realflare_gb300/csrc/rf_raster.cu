@@ -47,6 +47,16 @@ namespace {
 #endif
 constexpr int kBatchRecords = RF_RASTER_BATCH;
 
+#ifdef RF_RASTER_STATS
+// Work counters of the statistics build (never compiled into the product library):
+// record iterations per 8 x 4 block, those of whole-block records, fragments, fragments of
+// whole-block records, block visits.
+__device__ unsigned long long g_raster_stats[5];
+#define RF_STAT(stmt) stmt
+#else
+#define RF_STAT(stmt)
+#endif
+
 struct alignas(16) Rec {
     int bb[4];       // xmin, xmax, ymin, ymax (first: read as one 16-byte vector)
     int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
@@ -338,6 +348,8 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
 
     const int S = p.S;
     const FragmentConsts fc = fcs;
+    RF_STAT(unsigned long long st_iter = 0; unsigned long long st_whole = 0; unsigned long long st_frag = 0;
+            unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0;)
     // accumulators of the 32 pixel blocks, [block * 3 + channel][lane]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
@@ -404,6 +416,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             if (lane == 0) blk = atomicAdd(&next_block[cur], 1);
             blk = __shfl_sync(0xffffffffu, blk, 0);
             if (blk >= 32) break;
+            RF_STAT(st_blocks += lane == 0;)
             const int x0 = tx * kTile + (blk & 3) * 8, y0 = ty * kTile + (blk >> 2) * 4;
             const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
@@ -446,6 +459,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                     const bool is_whole = (whole[m] >> b) & 1u;
                     bits &= bits - 1;
                     const Rec& r = recs[j];
+                    RF_STAT(if (lane == 0) { st_iter++; st_whole += is_whole; })
                     if (!in_image) continue;
                     int hits = S;
                     if (!is_whole) {
@@ -457,6 +471,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
                         for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
                         if (hits == 0) continue;
                     }
+                    RF_STAT(st_frag++; st_frag_whole += is_whole;)
                     float wt[4];
                     barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
                     const float f = fragment_fast(r, wt, ghost, p, fc, hits);
@@ -482,6 +497,9 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
         __syncthreads();
     }
 
+    RF_STAT(atomicAdd(&g_raster_stats[0], st_iter); atomicAdd(&g_raster_stats[1], st_whole);
+            atomicAdd(&g_raster_stats[2], st_frag); atomicAdd(&g_raster_stats[3], st_frag_whole);
+            atomicAdd(&g_raster_stats[4], st_blocks);)
     __syncthreads();  // every block's last batch is shaded
     const float scale = p.intensity / (float)(p.W * p.S * p.WS);
 #pragma unroll
@@ -648,3 +666,17 @@ extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int
                                                            p, fragment_consts(p), (float4*)image);
     return launch_status();
 }
+
+#ifdef RF_RASTER_STATS
+// Statistics build only: read (and zero) the counters of the k_raster launches since the
+// last call. out: record iterations, whole-block record iterations, fragments, fragments of
+// whole-block records, block visits.
+extern "C" int rf_raster_stats(unsigned long long* out) {
+    using namespace rf;
+    if (!out) return RF_ERR_INVALID_ARG;
+    RF_TRY(cuda_status(cudaMemcpyFromSymbol(out, g_raster_stats, sizeof(unsigned long long) * 5)));
+    const unsigned long long zero[5] = {0, 0, 0, 0, 0};
+    RF_TRY(cuda_status(cudaMemcpyToSymbol(g_raster_stats, zero, sizeof zero)));
+    return RF_OK;
+}
+#endif
