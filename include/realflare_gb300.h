@@ -241,6 +241,82 @@ int rf_aperture_dust(float* image, int32_t width, int32_t height, float size_x, 
 int rf_aperture_noise_dust(float* image, const float* noise, float* scratch, int32_t width,
                            int32_t height, float strength, float sigma, void* stream);
 
+/* ---- batched frames ------------------------------------------------------------------ */
+/* Many frames (lights, lenses, grids, wavelength sets) in one launch per stage, with no
+ * host synchronisation, so the whole sequence can be captured into one CUDA graph. There
+ * is no reference counterpart: the reference renders one light per Engine call, and its
+ * only many-light path loops over lights in Python (realflare/api/engine.py:98-155). Each
+ * frame's results equal those of the single-frame functions on the same inputs. */
+typedef struct rf_frame {
+    rf_trace_args trace;      /* as for rf_trace */
+    rf_raster_args raster;    /* as for rf_raster; raster.tile_size is set by rf_batch_plan */
+    float area_orig, min_area;  /* as for rf_quad_setup */
+    int32_t element_offset;   /* first element in the concatenated rf_lens_element array */
+    int32_t path_offset;      /* first path (int32 pair) in the concatenated paths */
+    int32_t wavelength_offset;  /* first wavelength in the concatenated wavelengths */
+    int64_t ghost_offset;     /* first float of the frame's ghost texture */
+    int64_t image_offset;     /* first pixel (4 floats) of the frame's image */
+    /* filled by rf_batch_plan */
+    int64_t ray_offset;       /* the frame's rays: RF_RAY_PLANES planes of n_rays at rays + 6 * ray_offset */
+    int64_t prim_offset;      /* the frame's bounds (float4) */
+    int64_t inten_offset;     /* the frame's intensities (float) */
+    int64_t vertex_offset;    /* the frame's vertices (n_rays + 1 of them) */
+    int64_t pair_offset;      /* the frame's (primitive, wavelength pair) counters */
+    int64_t trace_block, quad_block, vertex_block, pair_block;  /* first block of each stage */
+    int32_t tile_offset, tile_count;  /* the frame's raster tiles in the batch's tile numbering */
+    float direction_n[3];     /* normalize(-direction.xyz) in FP32, as rf_trace computes it */
+    int32_t pad1;
+} rf_frame;
+
+typedef struct rf_batch_sizes {
+    int32_t frame_count, tile_size, rays_per_thread, tiles;
+    int64_t rays, prims, intensities, vertices, pairs;  /* element counts of the buffers */
+    int64_t trace_blocks, quad_blocks, vertex_blocks, pair_blocks;
+    int64_t image_pixels, ghost_floats;
+    int32_t max_colors, max_sub;  /* largest max(W-1,1) * WS and WS over the frames */
+} rf_batch_sizes;
+
+/* Checks every frame and fills the derived fields of frames (host memory) and sizes.
+ * tile_size: 16 or 32; rays_per_thread: 1, 2 or 4. The caller then copies frames to the
+ * device and allocates rays float[6 * sizes.rays], bounds float4[sizes.prims],
+ * intensities float[sizes.intensities], vertexes float[8 * sizes.vertices], images
+ * float[4 * sizes.image_pixels]. */
+int rf_batch_plan(rf_frame* frames, int32_t frame_count, int32_t tile_size, int32_t rays_per_thread,
+                  rf_batch_sizes* sizes);
+
+/* rf_trace of every frame: frames is the planned array in device memory; elements, paths
+ * and wavelengths are the concatenated inputs the frames' offsets index. */
+int rf_trace_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const rf_lens_element* elements,
+                   const int32_t* paths, const float* wavelengths, float* rays, void* stream);
+
+/* rf_quad_setup and rf_vertex of every frame. */
+int rf_quad_setup_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* rays,
+                        float* bounds, float* intensities, void* stream);
+int rf_vertex_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* rays,
+                    const float* intensities, float* vertexes, void* stream);
+
+/* Scratch bytes of rf_bin_tiles_batch + rf_raster_batch for an entry capacity. */
+int rf_batch_workspace_size(const rf_batch_sizes* sizes, int64_t entry_capacity, size_t* bytes);
+
+/* rf_bin_tiles of every frame into one tile numbering (frame f's tiles are tile_offset ..
+ * tile_offset + tile_count - 1), without host synchronisation: the entry total is written
+ * to entry_total (device uint64). When it exceeds entry_capacity the lists are incomplete,
+ * rf_raster_batch leaves the images untouched, and the caller retries with a larger
+ * capacity. Also orders the tiles by decreasing entry count for rf_raster_batch.
+ * tile_offsets: device uint32[tiles + 1]; tile_entries: device uint32[entry_capacity]. */
+int rf_bin_tiles_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* bounds,
+                       const float* vertexes, void* workspace, size_t workspace_bytes,
+                       uint32_t* tile_offsets, uint32_t* tile_entries, int64_t entry_capacity,
+                       uint64_t* entry_total, void* stream);
+
+/* rf_raster of every frame in one persistent launch: CTAs take tiles from a device-side
+ * queue (heaviest first) until it is empty. ghosts: the concatenated ghost textures;
+ * images: float[4 * image_pixels]; workspace: the one given to rf_bin_tiles_batch. */
+int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* vertexes,
+                    const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
+                    const float* spectrum, void* workspace, size_t workspace_bytes,
+                    int64_t entry_capacity, const uint64_t* entry_total, float* images, void* stream);
+
 /* ---- compositing ---------------------------------------------------------------------- */
 /* out = a * wa + b * wb elementwise over n floats (Engine.flare_starburst,
  * realflare/api/engine.py:174-187, uses wa = 2, wb = 1). */

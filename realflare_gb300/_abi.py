@@ -84,6 +84,57 @@ class StarburstArgs(ctypes.Structure):
     ]
 
 
+class Frame(ctypes.Structure):
+    """rf_frame: one frame of a batched render."""
+    _fields_ = [
+        ('trace', TraceArgs),
+        ('raster', RasterArgs),
+        ('area_orig', ctypes.c_float),
+        ('min_area', ctypes.c_float),
+        ('element_offset', ctypes.c_int32),
+        ('path_offset', ctypes.c_int32),
+        ('wavelength_offset', ctypes.c_int32),
+        ('ghost_offset', ctypes.c_int64),
+        ('image_offset', ctypes.c_int64),
+        ('ray_offset', ctypes.c_int64),
+        ('prim_offset', ctypes.c_int64),
+        ('inten_offset', ctypes.c_int64),
+        ('vertex_offset', ctypes.c_int64),
+        ('pair_offset', ctypes.c_int64),
+        ('trace_block', ctypes.c_int64),
+        ('quad_block', ctypes.c_int64),
+        ('vertex_block', ctypes.c_int64),
+        ('pair_block', ctypes.c_int64),
+        ('tile_offset', ctypes.c_int32),
+        ('tile_count', ctypes.c_int32),
+        ('direction_n', ctypes.c_float * 3),
+        ('pad1', ctypes.c_int32),
+    ]
+
+
+class BatchSizes(ctypes.Structure):
+    """rf_batch_sizes."""
+    _fields_ = [
+        ('frame_count', ctypes.c_int32),
+        ('tile_size', ctypes.c_int32),
+        ('rays_per_thread', ctypes.c_int32),
+        ('tiles', ctypes.c_int32),
+        ('rays', ctypes.c_int64),
+        ('prims', ctypes.c_int64),
+        ('intensities', ctypes.c_int64),
+        ('vertices', ctypes.c_int64),
+        ('pairs', ctypes.c_int64),
+        ('trace_blocks', ctypes.c_int64),
+        ('quad_blocks', ctypes.c_int64),
+        ('vertex_blocks', ctypes.c_int64),
+        ('pair_blocks', ctypes.c_int64),
+        ('image_pixels', ctypes.c_int64),
+        ('ghost_floats', ctypes.c_int64),
+        ('max_colors', ctypes.c_int32),
+        ('max_sub', ctypes.c_int32),
+    ]
+
+
 P = ctypes.c_void_p
 I32 = ctypes.c_int32
 I64 = ctypes.c_int64
@@ -110,6 +161,13 @@ SIGNATURES = {
     'rf_aperture_dust': [P, I32, I32, F32, F32, F32, F32, F32, F32, F32, F32, P],
     'rf_aperture_noise_dust': [P, P, P, I32, I32, F32, F32, P],
     'rf_axpby': [P, F32, P, F32, P, I64, P],
+    'rf_batch_plan': [ctypes.POINTER(Frame), I32, I32, I32, ctypes.POINTER(BatchSizes)],
+    'rf_trace_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P, P],
+    'rf_quad_setup_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P],
+    'rf_vertex_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P],
+    'rf_batch_workspace_size': [ctypes.POINTER(BatchSizes), I64, ctypes.POINTER(ctypes.c_size_t)],
+    'rf_bin_tiles_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, ctypes.c_size_t, P, P, I64, P, P],
+    'rf_raster_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P, P, P, ctypes.c_size_t, I64, P, P, P],
 }
 
 _lib = None

@@ -31,6 +31,7 @@ UNITS = {
     'rf_raster.cu': [],
     'rf_fft.cu': [],
     'rf_image.cu': [],
+    'rf_batch.cu': [],
 }
 
 

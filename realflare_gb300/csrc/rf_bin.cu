@@ -172,10 +172,11 @@ __global__ void k_tile_offsets(const uint32_t* __restrict__ keys, long long n, i
     tile_offsets[t] = (uint32_t)lo;
 }
 
-// The raster tile is 32 x 32 pixels (rf_raster.cu); bins must be multiples of it.
-int auto_tile(const rf_raster_args& a) { return a.tile_size > 0 ? a.tile_size : 32; }
+// Raster tiles are 32 x 32 (default) or 16 x 16 pixels (rf_raster.cu); bins must be
+// multiples of the tile.
+__host__ __device__ inline int auto_tile(const rf_raster_args& a) { return a.tile_size > 0 ? a.tile_size : 32; }
 
-bool make_geometry(const rf_raster_args& a, BinGeometry& g) {
+__host__ __device__ inline bool make_geometry(const rf_raster_args& a, BinGeometry& g) {
     if (a.width < 1 || a.height < 1 || a.bin_size < 1 || a.grid_count < 2 || a.wavelength_count < 1 ||
         a.path_count < 0)
         return false;
@@ -183,7 +184,7 @@ bool make_geometry(const rf_raster_args& a, BinGeometry& g) {
     g.height = a.height;
     g.B = a.bin_size;
     g.T = auto_tile(a);
-    if (g.T != 32 || g.B % g.T) return false;
+    if ((g.T != 32 && g.T != 16) || g.B % g.T) return false;
     g.bdx = (a.width + g.B - 1) / g.B;
     g.bdy = (a.height + g.B - 1) / g.B;
     g.ntx = (a.width + g.T - 1) / g.T;
@@ -195,6 +196,100 @@ bool make_geometry(const rf_raster_args& a, BinGeometry& g) {
     g.st = a.screen_transform;
     g.safe_screen = (float)a.width * a.sub_steps <= 16384.0f && (float)a.height * a.sub_steps <= 16384.0f;
     return true;
+}
+
+// ---------------------------------------------------------------- batched frames
+// Block b of a stage works for the frame whose first block is the largest one <= b; the
+// frame's pairs, bounds and vertices are found through its offsets, and its tiles are
+// numbered from tile_offset in the batch's tile numbering.
+struct FramePairs {
+    BinGeometry g;
+    long long n_pairs, first;  // the frame's pair count and this thread's first local pair
+    const float4* bounds;
+    const float4* vtx;
+    long long pair_offset;
+    int tile_offset;
+};
+
+__device__ __forceinline__ bool frame_pairs(const rf_frame* __restrict__ frames, int F, const float4* bounds_all,
+                                            const float4* vtx_all, int* frame_index, FramePairs& fp) {
+    if (threadIdx.x == 0)
+        *frame_index = find_frame(frames, F, blockIdx.x, [](const rf_frame& fr) { return fr.pair_block; });
+    __syncthreads();
+    const rf_frame& fr = frames[*frame_index];
+    if (!make_geometry(fr.raster, fp.g)) return false;
+    fp.n_pairs = (long long)fr.raster.path_count * (fp.g.G - 1) * (fp.g.G - 1) * fp.g.maxW;
+    fp.first = (long long)(blockIdx.x - fr.pair_block) * kThreads + threadIdx.x;
+    fp.bounds = bounds_all + fr.prim_offset;
+    fp.vtx = vtx_all + 2 * fr.vertex_offset;
+    fp.pair_offset = fr.pair_offset;
+    fp.tile_offset = fr.tile_offset;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads) k_pair_count_batch(const rf_frame* __restrict__ frames, int F,
+                                                               const float4* __restrict__ bounds_all,
+                                                               const float4* __restrict__ vtx_all,
+                                                               uint32_t* __restrict__ counts,
+                                                               unsigned long long* __restrict__ total) {
+    __shared__ int frame_index;
+    FramePairs fp;
+    const bool ok = frame_pairs(frames, F, bounds_all, vtx_all, &frame_index, fp);
+    const long long j = fp.first;
+    unsigned long long c = 0;
+    if (ok && j < fp.n_pairs) {
+        int tx0, tx1, ty0, ty1;
+        if (pair_tile_rect(fp.bounds, fp.vtx, j / fp.g.maxW, (int)(j % fp.g.maxW), fp.g, tx0, tx1, ty0, ty1))
+            c = (unsigned long long)(tx1 - tx0 + 1) * (unsigned long long)(ty1 - ty0 + 1);
+        counts[fp.pair_offset + j] = (uint32_t)min(c, 0xffffffffull);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
+}
+
+__global__ void __launch_bounds__(kThreads) k_pair_emit_batch(const rf_frame* __restrict__ frames, int F,
+                                                              const float4* __restrict__ bounds_all,
+                                                              const float4* __restrict__ vtx_all,
+                                                              const uint32_t* __restrict__ offsets,
+                                                              long long capacity, uint32_t* __restrict__ keys,
+                                                              uint32_t* __restrict__ vals) {
+    __shared__ int frame_index;
+    FramePairs fp;
+    if (!frame_pairs(frames, F, bounds_all, vtx_all, &frame_index, fp)) return;
+    const long long j = fp.first;
+    if (j >= fp.n_pairs) return;
+    int tx0, tx1, ty0, ty1;
+    if (!pair_tile_rect(fp.bounds, fp.vtx, j / fp.g.maxW, (int)(j % fp.g.maxW), fp.g, tx0, tx1, ty0, ty1)) return;
+    long long o = offsets[fp.pair_offset + j];
+    for (int ty = ty0; ty <= ty1; ty++)
+        for (int tx = tx0; tx <= tx1; tx++) {
+            if (o < capacity) {  // an overflowing batch is reported through the entry total
+                keys[o] = (uint32_t)(fp.tile_offset + ty * fp.g.ntx + tx);
+                vals[o] = (uint32_t)j;
+            }
+            o++;
+        }
+}
+
+// Entries [total, capacity) get the key `pad` (one past the last tile), so the sort over the
+// whole capacity leaves them at the end.
+__global__ void k_pad_entries(const unsigned long long* __restrict__ total, long long capacity, uint32_t pad,
+                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= capacity || (unsigned long long)i < *total) return;
+    keys[i] = pad;
+    vals[i] = 0;
+}
+
+// Sort keys for the raster's work queue: the number of leading zeros of the tile's entry
+// count (heaviest tiles first; empty tiles, which still write their pixels, last).
+__global__ void k_tile_order_keys(const uint32_t* __restrict__ tile_offsets, int tiles, uint32_t* __restrict__ keys,
+                                  uint32_t* __restrict__ vals) {
+    const int t = blockIdx.x * kThreads + threadIdx.x;
+    if (t >= tiles) return;
+    keys[t] = (uint32_t)__clz((int)(tile_offsets[t + 1] - tile_offsets[t]));
+    vals[t] = (uint32_t)t;
 }
 
 struct BinWorkspace {
@@ -225,6 +320,36 @@ BinWorkspace layout(char* base, long long n_pairs, long long capacity) {
 }  // namespace
 
 int tile_size_of(const rf_raster_args& a) { return auto_tile(a); }
+
+BatchWorkspace batch_layout(char* base, const rf_batch_sizes& z, long long capacity) {
+    BatchWorkspace w;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    const long long sort_n = capacity > z.tiles ? capacity : z.tiles;
+    w.counts = (uint32_t*)take(sizeof(uint32_t) * (size_t)(z.pairs + 1));
+    w.scan_scratch = (uint32_t*)take(sizeof(uint32_t) * scan_scratch_words(z.pairs));
+    w.keys_a = (uint32_t*)take(sizeof(uint32_t) * (size_t)capacity);
+    w.keys_b = (uint32_t*)take(sizeof(uint32_t) * (size_t)capacity);
+    w.vals_tmp = (uint32_t*)take(sizeof(uint32_t) * (size_t)capacity);
+    w.radix_scratch = (uint32_t*)take(sizeof(uint32_t) * radix_scratch_words(sort_n));
+    w.order_keys = (uint32_t*)take(sizeof(uint32_t) * (size_t)z.tiles);
+    w.order_vals = (uint32_t*)take(sizeof(uint32_t) * (size_t)z.tiles);
+    w.order_keys_b = (uint32_t*)take(sizeof(uint32_t) * (size_t)z.tiles);
+    w.order_vals_b = (uint32_t*)take(sizeof(uint32_t) * (size_t)z.tiles);
+    w.queue = (uint32_t*)take(sizeof(uint32_t) * 4);
+    w.bytes = off;
+    return w;
+}
+
+// The tile order is sorted by 6-bit keys: one pass when there are two tiles or more, so it
+// starts in the _b buffers and ends in order_vals; a single tile is never moved.
+const uint32_t* batch_tile_order(const BatchWorkspace& w, const rf_batch_sizes& z) {
+    return z.tiles > 1 ? w.order_vals : w.order_vals_b;
+}
 
 }  // namespace rf
 
@@ -315,4 +440,64 @@ extern "C" int rf_bin_tiles(const float* bounds, const float* vertexes, const rf
     k_tile_offsets<<<blocks_for(ntiles + 1, kThreads), kThreads, 0, s>>>(sorted_keys, (long long)total, ntiles,
                                                                           tile_offsets);
     return launch_status();
+}
+
+extern "C" int rf_batch_workspace_size(const rf_batch_sizes* sizes, int64_t entry_capacity, size_t* bytes) {
+    using namespace rf;
+    if (!sizes || !bytes || entry_capacity < 0) return RF_ERR_INVALID_ARG;
+    *bytes = batch_layout(nullptr, *sizes, entry_capacity).bytes;
+    return RF_OK;
+}
+
+extern "C" int rf_bin_tiles_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* bounds,
+                                  const float* vertexes, void* workspace, size_t workspace_bytes,
+                                  uint32_t* tile_offsets, uint32_t* tile_entries, int64_t entry_capacity,
+                                  uint64_t* entry_total, void* stream) {
+    using namespace rf;
+    if (!frames || !sizes || !bounds || !vertexes || !workspace || !tile_offsets || !entry_total ||
+        entry_capacity < 1 || !tile_entries)
+        return RF_ERR_INVALID_ARG;
+    if (!aligned16(bounds) || !aligned16(vertexes) || !aligned16(workspace)) return RF_ERR_INVALID_ARG;
+    const rf_batch_sizes& z = *sizes;
+    if (entry_capacity > 0xfffffff0LL || z.tiles < 1 || z.tiles > (1 << 30) || z.pair_blocks > 0x7fffffffLL)
+        return RF_ERR_NOT_SUPPORTED;
+    BatchWorkspace w = batch_layout((char*)workspace, z, entry_capacity);
+    if (w.bytes > workspace_bytes) return RF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    RF_TRY(cuda_status(cudaMemsetAsync(entry_total, 0, sizeof(uint64_t), s)));
+    if (z.pair_blocks > 0) {
+        k_pair_count_batch<<<(unsigned)z.pair_blocks, kThreads, 0, s>>>(
+            frames, z.frame_count, (const float4*)bounds, (const float4*)vertexes, w.counts,
+            (unsigned long long*)entry_total);
+        RF_TRY(launch_status());
+        RF_TRY(exclusive_scan_u32(w.counts, w.counts, z.pairs, w.scan_scratch, s));
+    }
+    int bits = 0;
+    while ((1LL << bits) <= z.tiles) bits++;  // keys 0 .. tiles (tiles = padding)
+    const int passes = (entry_capacity > 1) ? (bits + 7) / 8 : 0;
+    uint32_t* vals_first = (passes % 2 == 0) ? tile_entries : w.vals_tmp;
+    uint32_t* vals_alt = (passes % 2 == 0) ? w.vals_tmp : tile_entries;
+    if (z.pair_blocks > 0) {
+        k_pair_emit_batch<<<(unsigned)z.pair_blocks, kThreads, 0, s>>>(
+            frames, z.frame_count, (const float4*)bounds, (const float4*)vertexes, w.counts, entry_capacity,
+            w.keys_a, vals_first);
+        RF_TRY(launch_status());
+    }
+    k_pad_entries<<<blocks_for(entry_capacity, kThreads), kThreads, 0, s>>>(
+        (const unsigned long long*)entry_total, entry_capacity, (uint32_t)z.tiles, w.keys_a, vals_first);
+    RF_TRY(launch_status());
+    bool in_alt = false;
+    RF_TRY(radix_sort_pairs(w.keys_a, vals_first, w.keys_b, vals_alt, entry_capacity, bits, w.radix_scratch,
+                            &in_alt, s));
+    const uint32_t* sorted_keys = in_alt ? w.keys_b : w.keys_a;
+    k_tile_offsets<<<blocks_for(z.tiles + 1, kThreads), kThreads, 0, s>>>(sorted_keys, entry_capacity, z.tiles,
+                                                                          tile_offsets);
+    RF_TRY(launch_status());
+    // the raster's work queue: tiles by decreasing entry count
+    k_tile_order_keys<<<blocks_for(z.tiles, kThreads), kThreads, 0, s>>>(tile_offsets, z.tiles, w.order_keys_b,
+                                                                         w.order_vals_b);
+    RF_TRY(launch_status());
+    RF_TRY(radix_sort_pairs(w.order_keys_b, w.order_vals_b, w.order_keys, w.order_vals, z.tiles, 6, w.radix_scratch,
+                            &in_alt, s));
+    return RF_OK;
 }

@@ -40,6 +40,21 @@ inline int cuda_status(cudaError_t e) {
 inline unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// ---------------------------------------------------------------- batched frames
+// The frame owning work unit `unit` of a stage: the last frame whose first unit of that
+// stage (first(frame), non-decreasing over the frames) is <= unit. Frames without units
+// share their first unit with the next frame, so the last of equal starts owns it.
+template <class First>
+__device__ __forceinline__ int find_frame(const rf_frame* __restrict__ frames, int F, long long unit, First first) {
+    int lo = 0, hi = F - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((long long)first(frames[mid]) <= unit) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------- integer semantics
 // float -> int truncating toward zero, saturating, NaN -> 0 (cvt.rzi.s32.f32 semantics,
 // the conversion the reference's convert_int2/convert_int4 compile to on NVIDIA GPUs).
@@ -94,6 +109,17 @@ __device__ __forceinline__ float4 xyz_to_ap1(float x, float y, float z) {
 
 // The n-rook sample offsets of realflare/api/tasks/rasterizing.py:78-87.
 __device__ __constant__ static const unsigned char SUB_OFFSETS[15] = {0, 1, 0, 1, 2, 0, 3, 4, 1, 6, 2, 5, 0, 3, 7};
+
+// ---------------------------------------------------------------- batch workspace
+// Scratch of rf_bin_tiles_batch and rf_raster_batch (rf_bin.cu): pair counters and their
+// scan, the entry sort's buffers, the raster's tile order and its queue head.
+struct BatchWorkspace {
+    uint32_t *counts, *scan_scratch, *keys_a, *keys_b, *vals_tmp, *radix_scratch;
+    uint32_t *order_keys, *order_vals, *order_keys_b, *order_vals_b, *queue;
+    size_t bytes;
+};
+BatchWorkspace batch_layout(char* base, const rf_batch_sizes& sizes, long long entry_capacity);
+const uint32_t* batch_tile_order(const BatchWorkspace& w, const rf_batch_sizes& sizes);
 
 // ---------------------------------------------------------------- scans / sorting
 // Exclusive prefix sum of n uint32 values (in may equal out). scratch: scan_scratch_words(n)

@@ -17,11 +17,11 @@ __device__ __forceinline__ float edge_f(float ax, float ay, float bx, float by, 
     return (ax - bx) * (cy - ay) - (ay - by) * (cx - ax);
 }
 
-__global__ void __launch_bounds__(kThreads) k_quad_setup(const float* __restrict__ rays, int P, int W, int G,
-                                                         long long n_rays, float area_orig, float min_area,
-                                                         float4* __restrict__ bounds, float* __restrict__ inten) {
+// Primitive pq = path * Q + quad of one frame.
+__device__ __forceinline__ void quad_setup_one(const float* __restrict__ rays, int P, int W, int G, long long n_rays,
+                                               float area_orig, float min_area, float4* __restrict__ bounds,
+                                               float* __restrict__ inten, long long pq) {
     const int Q = (G - 1) * (G - 1), R = G * G;
-    const long long pq = (long long)blockIdx.x * kThreads + threadIdx.x;
     if (pq >= (long long)P * Q) return;
     const int path = (int)(pq / Q), quad = (int)(pq % Q);
     const int row = quad / (G - 1), col = quad % (G - 1);
@@ -88,11 +88,18 @@ __global__ void __launch_bounds__(kThreads) k_quad_setup(const float* __restrict
     bounds[pq] = make_float4(culled ? __int_as_float(0x7fffffff) : bx0, by0, bx1, by1);
 }
 
-__global__ void __launch_bounds__(kThreads) k_vertex(const float* __restrict__ rays, const float* __restrict__ inten,
-                                                     int P, int W, int G, long long n_rays, float st, float half_w,
-                                                     float half_h, float4* __restrict__ vertexes) {
+__global__ void __launch_bounds__(kThreads) k_quad_setup(const float* __restrict__ rays, int P, int W, int G,
+                                                         long long n_rays, float area_orig, float min_area,
+                                                         float4* __restrict__ bounds, float* __restrict__ inten) {
+    quad_setup_one(rays, P, W, G, n_rays, area_orig, min_area, bounds, inten,
+                   (long long)blockIdx.x * kThreads + threadIdx.x);
+}
+
+// Vertex i (ray-plane order; i == n_rays is the trailing zero vertex) of one frame.
+__device__ __forceinline__ void vertex_one(const float* __restrict__ rays, const float* __restrict__ inten, int P,
+                                           int W, int G, long long n_rays, float st, float half_w, float half_h,
+                                           float4* __restrict__ vertexes, long long i) {
     const int Q = (G - 1) * (G - 1), R = G * G;
-    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;  // ray-plane order
     if (i > n_rays) return;
     if (i == n_rays) {  // the zero vertex after the last one
         vertexes[2 * n_rays] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -136,6 +143,48 @@ __global__ void __launch_bounds__(kThreads) k_vertex(const float* __restrict__ r
     vertexes[2 * vi + 1] = b;
 }
 
+__global__ void __launch_bounds__(kThreads) k_vertex(const float* __restrict__ rays, const float* __restrict__ inten,
+                                                     int P, int W, int G, long long n_rays, float st, float half_w,
+                                                     float half_h, float4* __restrict__ vertexes) {
+    vertex_one(rays, inten, P, W, G, n_rays, st, half_w, half_h, vertexes,
+               (long long)blockIdx.x * kThreads + threadIdx.x);
+}
+
+// Batched forms: block b works for the frame whose first block of the stage is the largest
+// one <= b.
+__global__ void __launch_bounds__(kThreads) k_quad_setup_batch(const rf_frame* __restrict__ frames, int F,
+                                                               const float* __restrict__ rays_all,
+                                                               float4* __restrict__ bounds_all,
+                                                               float* __restrict__ inten_all) {
+    __shared__ int frame_index;
+    if (threadIdx.x == 0)
+        frame_index = find_frame(frames, F, blockIdx.x, [](const rf_frame& fr) { return fr.quad_block; });
+    __syncthreads();
+    const rf_frame& fr = frames[frame_index];
+    const int P = fr.trace.path_count, W = fr.trace.wavelength_count, G = fr.trace.grid_count;
+    const long long n_rays = (long long)P * W * G * G;
+    quad_setup_one(rays_all + 6 * fr.ray_offset, P, W, G, n_rays, fr.area_orig, fr.min_area,
+                   bounds_all + fr.prim_offset, inten_all + fr.inten_offset,
+                   (long long)(blockIdx.x - fr.quad_block) * kThreads + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kThreads) k_vertex_batch(const rf_frame* __restrict__ frames, int F,
+                                                           const float* __restrict__ rays_all,
+                                                           const float* __restrict__ inten_all,
+                                                           float4* __restrict__ vertexes_all) {
+    __shared__ int frame_index;
+    if (threadIdx.x == 0)
+        frame_index = find_frame(frames, F, blockIdx.x, [](const rf_frame& fr) { return fr.vertex_block; });
+    __syncthreads();
+    const rf_frame& fr = frames[frame_index];
+    const int P = fr.trace.path_count, W = fr.trace.wavelength_count, G = fr.trace.grid_count;
+    const long long n_rays = (long long)P * W * G * G;
+    const float half_w = (float)fr.raster.width / 2.0f, half_h = (float)fr.raster.height / 2.0f;
+    vertex_one(rays_all + 6 * fr.ray_offset, inten_all + fr.inten_offset, P, W, G, n_rays,
+               fr.raster.screen_transform, half_w, half_h, vertexes_all + 2 * fr.vertex_offset,
+               (long long)(blockIdx.x - fr.vertex_block) * kThreads + threadIdx.x);
+}
+
 }  // namespace
 }  // namespace rf
 
@@ -168,5 +217,29 @@ extern "C" int rf_vertex(const float* rays, const float* intensities, int32_t pa
     k_vertex<<<blocks_for(n_rays + 1, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
         rays, intensities, path_count, wavelength_count, grid_count, n_rays, screen_transform, half_w, half_h,
         (float4*)vertexes);
+    return launch_status();
+}
+
+extern "C" int rf_quad_setup_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* rays,
+                                   float* bounds, float* intensities, void* stream) {
+    using namespace rf;
+    if (!frames || !sizes || !rays || !bounds || !intensities) return RF_ERR_INVALID_ARG;
+    if (!aligned16(bounds)) return RF_ERR_INVALID_ARG;
+    if (sizes->quad_blocks == 0) return RF_OK;
+    if (sizes->quad_blocks > 0x7fffffffLL) return RF_ERR_NOT_SUPPORTED;
+    k_quad_setup_batch<<<(unsigned)sizes->quad_blocks, kThreads, 0, (cudaStream_t)stream>>>(
+        frames, sizes->frame_count, rays, (float4*)bounds, intensities);
+    return launch_status();
+}
+
+extern "C" int rf_vertex_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* rays,
+                               const float* intensities, float* vertexes, void* stream) {
+    using namespace rf;
+    if (!frames || !sizes || !rays || !intensities || !vertexes) return RF_ERR_INVALID_ARG;
+    if (!aligned16(vertexes)) return RF_ERR_INVALID_ARG;
+    if (sizes->vertex_blocks == 0) return RF_OK;
+    if (sizes->vertex_blocks > 0x7fffffffLL) return RF_ERR_NOT_SUPPORTED;
+    k_vertex_batch<<<(unsigned)sizes->vertex_blocks, kThreads, 0, (cudaStream_t)stream>>>(
+        frames, sizes->frame_count, rays, intensities, (float4*)vertexes);
     return launch_status();
 }

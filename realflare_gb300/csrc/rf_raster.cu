@@ -23,6 +23,9 @@
 // parity checks of the binner and the rasteriser.
 #include <stddef.h>
 
+#include <algorithm>
+#include <atomic>
+
 #include "rf_common.cuh"
 
 namespace rf {
@@ -236,7 +239,7 @@ __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], c
     return gi * ri * ai * ci * (float)hits;
 }
 
-inline FragmentConsts fragment_consts(const RasterParams& p) {
+__host__ __device__ inline FragmentConsts fragment_consts(const RasterParams& p) {
     FragmentConsts fc;
     const double sx = 0.5 / p.ghost_scale * p.ghost_w, sy = 0.5 / p.ghost_scale * p.ghost_h;
     fc.tsx = (float)sx;
@@ -303,26 +306,31 @@ __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int 
     r.color = w * p.WS + i;
 }
 
-// One CTA per 32 x 32 tile, 8 warps; warp w shades the four 8 x 4 pixel blocks
-// w, w + 8, w + 16, w + 24 (block b at column b % 4, row b / 4), so a record outside a
-// block's sample bounds is skipped by the whole warp at once.
-constexpr int kTile = 32;
+// A CTA of 8 warps shades one T x T tile (T = 32 or 16): the tile's T^2 / 32 blocks of
+// 8 x 4 pixels (block b at column b % (T / 8), row b / (T / 8)) go to warps one at a time,
+// so a record outside a block's sample bounds is skipped by the whole warp at once.
 constexpr int kThreads = 256;
 
-__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const float4* __restrict__ vtx,
-                                                       const uint32_t* __restrict__ tile_offsets,
-                                                       const uint32_t* __restrict__ tile_entries,
-                                                       const float* __restrict__ ghost,
-                                                       const float* __restrict__ spectrum, RasterParams p,
-                                                       FragmentConsts fcs, float4* __restrict__ image) {
-    extern __shared__ float4 smem4[];
-    __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
+template <int T>
+constexpr size_t raster_smem_bytes(int maxW, int WS) {
+    return sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * maxW * WS + ((WS + 3) & ~3)) +
+           sizeof(float) * 96 * (T * T / 32);
+}
+
+// Tile (tx, ty), whose entries are tile_entries[begin, end). smem4 holds the dynamic shared
+// memory (raster_smem_bytes), next_block two shared counters.
+template <int T>
+__device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint32_t begin, uint32_t end,
+                                            const uint32_t* __restrict__ tile_entries,
+                                            const float* __restrict__ ghost, const float* __restrict__ spectrum,
+                                            const RasterParams& p, const FragmentConsts& fcs,
+                                            float4* __restrict__ image, int tx, int ty, float4* smem4,
+                                            int* next_block) {
+    constexpr int kBlocks = T * T / 32;  // 8 x 4 pixel blocks per tile
+    constexpr int kCols = T / 8;         // blocks per tile row
     Rec* recbuf = (Rec*)smem4;     // two batches of records
     float* xyz = (float*)(recbuf + 2 * kBatchRecords);  // [maxW * WS][3]
     float* blend = xyz + 3 * p.maxW * p.WS;       // [WS]
-
-    const int tile = blockIdx.x;
-    const int tx = tile % p.ntx, ty = tile / p.ntx;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
@@ -350,12 +358,11 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
     const FragmentConsts fc = fcs;
     RF_STAT(unsigned long long st_iter = 0; unsigned long long st_whole = 0; unsigned long long st_frag = 0;
             unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0;)
-    // accumulators of the 32 pixel blocks, [block * 3 + channel][lane]
+    // accumulators of the pixel blocks, [block * 3 + channel][lane]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
-    for (int c = 0; c < 12; c++) acc[c * kThreads + threadIdx.x] = 0.0f;
+    for (int i = threadIdx.x; i < kBlocks * 96; i += kThreads) acc[i] = 0.0f;
 
-    const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
     const int per_batch = kBatchRecords / p.WS;  // entries per batch (WS <= kBatchRecords)
     // Batches of records are double-buffered: while warps shade batch t from one buffer,
     // warps that are done build batch t + 1 in the other, one barrier per batch. Thread j
@@ -415,9 +422,9 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
             int blk = 0;
             if (lane == 0) blk = atomicAdd(&next_block[cur], 1);
             blk = __shfl_sync(0xffffffffu, blk, 0);
-            if (blk >= 32) break;
+            if (blk >= kBlocks) break;
             RF_STAT(st_blocks += lane == 0;)
-            const int x0 = tx * kTile + (blk & 3) * 8, y0 = ty * kTile + (blk >> 2) * 4;
+            const int x0 = tx * T + (blk % kCols) * 8, y0 = ty * T + (blk / kCols) * 4;
             const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
             const bool in_image = px < p.width && py < p.height;
@@ -503,15 +510,65 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS) k_raster(const
     __syncthreads();  // every block's last batch is shaded
     const float scale = p.intensity / (float)(p.W * p.S * p.WS);
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < kBlocks / 8; k++) {
         const int blk = warp + 8 * k;
-        const int px = tx * kTile + (blk & 3) * 8 + (lane & 7), py = ty * kTile + (blk >> 2) * 4 + (lane >> 3);
+        const int px = tx * T + (blk % kCols) * 8 + (lane & 7), py = ty * T + (blk / kCols) * 4 + (lane >> 3);
         if (px >= p.width || py >= p.height) continue;
         const float c0 = acc[(3 * blk) * 32 + lane], c1 = acc[(3 * blk + 1) * 32 + lane],
                     c2 = acc[(3 * blk + 2) * 32 + lane];
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c0 > 0.0f || c1 > 0.0f || c2 > 0.0f) out = xyz_to_ap1(c0 * scale, c1 * scale, c2 * scale);
         image[(size_t)(p.height - (py + 1)) * p.width + px] = out;
+    }
+}
+
+// One CTA per tile of a frame.
+template <int T>
+__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
+    k_raster(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
+             const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
+             const float* __restrict__ spectrum, RasterParams p, FragmentConsts fcs, float4* __restrict__ image) {
+    extern __shared__ float4 smem4[];
+    __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
+    const int tile = blockIdx.x;
+    raster_tile<T>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs, image,
+                   tile % p.ntx, tile / p.ntx, smem4, next_block);
+}
+
+__host__ __device__ inline bool make_params(const rf_raster_args& a, RasterParams& p);
+__host__ __device__ inline FragmentConsts fragment_consts(const RasterParams& p);
+
+// Every frame of a batch in one persistent launch: each CTA takes the next tile from the
+// queue (tiles ordered by decreasing entry count) until none are left.
+template <int T>
+__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
+    k_raster_batch(const rf_frame* __restrict__ frames, int F, int tiles, const uint32_t* __restrict__ order,
+                   unsigned* __restrict__ queue, const unsigned long long* __restrict__ entry_total,
+                   long long capacity, const float4* __restrict__ vtx_all, const uint32_t* __restrict__ tile_offsets,
+                   const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghosts,
+                   const float* __restrict__ spectrum, float4* __restrict__ images) {
+    extern __shared__ float4 smem4[];
+    __shared__ int next_block[2];
+    __shared__ int item;
+    if (*entry_total > (unsigned long long)capacity) return;  // incomplete lists: nothing is drawn
+    for (;;) {
+        if (threadIdx.x == 0) item = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int it = item;
+        if (it >= tiles) break;
+        const int gt = (int)order[it];
+        const int f = find_frame(frames, F, gt, [](const rf_frame& fr) { return fr.tile_offset; });
+        const rf_frame& fr = frames[f];
+        RasterParams p;
+        make_params(fr.raster, p);
+        p.T = T;
+        p.ntx = (p.width + T - 1) / T;
+        const FragmentConsts fc = fragment_consts(p);
+        const int tile = gt - fr.tile_offset;
+        raster_tile<T>(vtx_all + 2 * fr.vertex_offset, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
+                       ghosts + fr.ghost_offset, spectrum, p, fc, images + fr.image_offset, tile % p.ntx,
+                       tile / p.ntx, smem4, next_block);
+        __syncthreads();  // the tile's accumulators and `item` are free again
     }
 }
 
@@ -603,7 +660,7 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
     image[(size_t)(p.height - (y + 1)) * p.width + x] = out;
 }
 
-bool make_params(const rf_raster_args& a, RasterParams& p) {
+__host__ __device__ inline bool make_params(const rf_raster_args& a, RasterParams& p) {
     if (a.width < 1 || a.height < 1 || a.grid_count < 2 || a.wavelength_count < 1 || a.wavelength_sub_count < 1 ||
         a.path_count < 0 || a.ghost_width < 1 || a.ghost_height < 1)
         return false;
@@ -623,22 +680,91 @@ bool make_params(const rf_raster_args& a, RasterParams& p) {
     return true;
 }
 
+// Raise a kernel's dynamic shared-memory limit once per device and size, so that later
+// launches of it can be captured into a CUDA graph without further attribute calls.
+constexpr int kMaxDevices = 64;
+template <class K>
+int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
+    if (bytes <= 48 * 1024) return RF_OK;
+    int dev = 0;
+    RF_TRY(cuda_status(cudaGetDevice(&dev)));
+    if (dev < 0 || dev >= kMaxDevices) return RF_ERR_NOT_SUPPORTED;
+    if (bytes <= allowed[dev].load()) return RF_OK;
+    RF_TRY(cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes)));
+    allowed[dev].store(bytes);
+    return RF_OK;
+}
+
+template <int T>
 int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
                   const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
-    p.T = kTile;
-    p.ntx = (p.width + kTile - 1) / kTile;
-    const int nty = (p.height + kTile - 1) / kTile;
-    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
-                        sizeof(float) * 12 * kThreads;
-    if (smem > 48 * 1024)
-        RF_TRY(cuda_status(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
-    k_raster<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum, p,
-                                                fragment_consts(p), (float4*)image);
+    static std::atomic<size_t> allowed[kMaxDevices];
+    p.T = T;
+    p.ntx = (p.width + T - 1) / T;
+    const int nty = (p.height + T - 1) / T;
+    const size_t smem = raster_smem_bytes<T>(p.maxW, p.WS);
+    RF_TRY(allow_smem(k_raster<T>, smem, allowed));
+    k_raster<T><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum, p,
+                                                   fragment_consts(p), (float4*)image);
+    return launch_status();
+}
+
+template <int T>
+int launch_raster_batch(const rf_frame* frames, const rf_batch_sizes& z, const float* vertexes,
+                        const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
+                        const float* spectrum, const BatchWorkspace& w, long long capacity,
+                        const uint64_t* entry_total, float* images, cudaStream_t s) {
+    static std::atomic<size_t> allowed[kMaxDevices];
+    static std::atomic<int> ctas_per_sm[kMaxDevices];
+    // the largest frame layout: 3 * max(W-1,1) * WS colours, WS blend weights (rounded to 4)
+    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * z.max_colors + ((z.max_sub + 3) & ~3)) +
+                        sizeof(float) * 96 * (T * T / 32);
+    RF_TRY(allow_smem(k_raster_batch<T>, smem, allowed));
+    int dev = 0, sms = 0;
+    RF_TRY(cuda_status(cudaGetDevice(&dev)));
+    RF_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)));
+    int per_sm = ctas_per_sm[dev].load();
+    if (per_sm == 0) {
+        RF_TRY(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_batch<T>, kThreads, smem)));
+        per_sm = per_sm > 0 ? per_sm : 1;
+        ctas_per_sm[dev].store(per_sm);
+    }
+    const long long ctas = std::min<long long>((long long)sms * per_sm, z.tiles);
+    RF_TRY(cuda_status(cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), s)));
+    k_raster_batch<T><<<(unsigned)ctas, kThreads, smem, s>>>(
+        frames, z.frame_count, z.tiles, batch_tile_order(w, z), w.queue, (const unsigned long long*)entry_total,
+        capacity, (const float4*)vertexes, tile_offsets, tile_entries, ghosts, spectrum, (float4*)images);
     return launch_status();
 }
 
 }  // namespace
 }  // namespace rf
+
+extern "C" int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* vertexes,
+                               const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
+                               const float* spectrum, void* workspace, size_t workspace_bytes,
+                               int64_t entry_capacity, const uint64_t* entry_total, float* images, void* stream) {
+    using namespace rf;
+    if (!frames || !sizes || !vertexes || !tile_offsets || !tile_entries || !ghosts || !spectrum || !workspace ||
+        !entry_total || !images || entry_capacity < 1)
+        return RF_ERR_INVALID_ARG;
+    if (!aligned16(vertexes) || !aligned16(images) || !aligned16(workspace)) return RF_ERR_INVALID_ARG;
+    const rf_batch_sizes& z = *sizes;
+    if (z.tiles < 1) return RF_OK;
+    if (z.max_sub < 1 || z.max_sub > kBatchRecords || z.max_colors > 4096) return RF_ERR_INVALID_ARG;
+    BatchWorkspace w = batch_layout((char*)workspace, z, entry_capacity);
+    if (w.bytes > workspace_bytes) return RF_ERR_INVALID_ARG;
+    switch (z.tile_size) {
+        case 32:
+            return launch_raster_batch<32>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum, w,
+                                           entry_capacity, entry_total, images, (cudaStream_t)stream);
+        case 16:
+            return launch_raster_batch<16>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum, w,
+                                           entry_capacity, entry_total, images, (cudaStream_t)stream);
+        default:
+            return RF_ERR_NOT_SUPPORTED;
+    }
+}
 
 extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
                          const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
@@ -649,8 +775,16 @@ extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, co
     RasterParams p;
     if (!make_params(*args, p)) return RF_ERR_INVALID_ARG;
     if (p.WS > kBatchRecords || p.maxW * p.WS > 4096) return RF_ERR_INVALID_ARG;
-    if (tile_size_of(*args) != kTile) return RF_ERR_NOT_SUPPORTED;
-    return launch_raster(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image, (cudaStream_t)stream);
+    switch (tile_size_of(*args)) {
+        case 32:
+            return launch_raster<32>(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image,
+                                     (cudaStream_t)stream);
+        case 16:
+            return launch_raster<16>(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image,
+                                     (cudaStream_t)stream);
+        default:
+            return RF_ERR_NOT_SUPPORTED;
+    }
 }
 
 extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_count, const float* ghost,

@@ -171,74 +171,35 @@ __device__ __forceinline__ float dispersion(float lambda, const float* c) {
     return sqrtf(1.0f + d0 + d1 + d2);
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace(const rf_lens_element* __restrict__ elements,
-                                                         const int2* __restrict__ paths,
-                                                         const float* __restrict__ wavelengths,
-                                                         const __grid_constant__ TraceParams p,
-                                                         float* __restrict__ rays) {
-    __shared__ SmemElement se[kMaxElements];
-    __shared__ float ior_tab[kMaxTableWavelengths * kMaxElements];
-    const int E = p.E;
-    const long long first = (long long)blockIdx.x * kTraceThreads;
-    // wavelength rows this block needs: the span of (first, last) ray indices
-    const long long last = min(first + kTraceThreads, p.n_rays) - 1;
-    const long long pw_first = first / p.R, pw_last = last / p.R;
-    const long long span_rows = pw_last - pw_first + 1;
-    const int span = (int)(span_rows < (long long)p.W ? span_rows : (long long)p.W);
-    const bool table = span <= kMaxTableWavelengths;
-    // dispersion is on unless coefficient 0 of element 0 is NaN (raytracing.cl:255)
-    const bool disperse = !isnan(__ldg(&elements[0].coefficients[0]));
-    for (int i = threadIdx.x; i < E; i += kTraceThreads) {
-        const rf_lens_element& e = elements[i];
-        se[i].radius = e.radius;
-        se[i].center = e.center;
-        se[i].height = e.height;
-        se[i].ior = e.ior;
-        se[i].coating = e.coating;
-        se[i].layers = e.coating_layers;
-        se[i].d0 = e.coating_thickness[0];
-        se[i].d1 = e.coating_thickness[1];
-    }
-    if (table) {
-        for (int k = threadIdx.x; k < span * E; k += kTraceThreads) {
-            int row = k / E, el = k % E;
-            int wl = (int)((pw_first + row) % p.W);
-            float n = elements[el].ior;
-            if (disperse && n > 1.0f) n = dispersion(wavelengths[wl], elements[el].coefficients);
-            ior_tab[row * E + el] = n;
-        }
-    }
-    __syncthreads();
+// Per-frame constants of the trace.
+struct TraceFrame {
+    int E, aperture, W, G, R;
+    float cmin, layer_n0, layer_n1;
+    float dir[3];  // normalize(-direction.xyz), host-computed in FP32
+};
 
-    const long long idx = first + threadIdx.x;
-    if (idx >= p.n_rays) return;
-    const int ray_id = (int)(idx % p.R);
-    const long long pw = idx / p.R;
-    const int wl_id = (int)(pw % p.W);
-    const int path_id = (int)(pw / p.W);
-    const int row = (int)((pw - pw_first) % p.W);
-    const int2 path = __ldg(paths + path_id);
-    const float wavelength = __ldg(wavelengths + wl_id);
-    const float* coef_base = &elements[0].coefficients[0];
-
+// One ray: init_ray (raytracing.cl:178-215) from grid point (grid_x, grid_y), then the
+// element loop of raytrace (218-359). ior_row: this ray's wavelength row of the (wavelength,
+// element) index table in shared memory, or nullptr to evaluate dispersion per element.
+__device__ __forceinline__ void trace_ray(const SmemElement* __restrict__ se, const float* ior_row, bool disperse,
+                                          const float* __restrict__ coef_base, float wavelength, int2 path,
+                                          float grid_x, float grid_y, const TraceFrame& f, float out[6]) {
+    const int E = f.E;
     auto ior_of = [&](int el) -> float {
-        if (table) return ior_tab[row * E + el];
+        if (ior_row) return ior_row[el];
         float n = se[el].ior;
         if (disperse && n > 1.0f) n = dispersion(wavelength, coef_base + (size_t)el * 16);
         return n;
     };
 
-    // init_ray, raytracing.cl:178-215
-    const int gy = (int)truncf((float)ray_id / (float)p.G);
-    const int gx = ray_id - gy * p.G;
-    float px = p.grid[gx], py = -p.grid[gy], pz = 1.0f;
+    float px = grid_x, py = -grid_y, pz = 1.0f;
     {
         Hit h0 = intersect(px, py, pz, 0.0f, 0.0f, -1.0f, se[0]);
         px = h0.px;  // zero when the grid point misses element 0
         py = h0.py;
         pz = h0.pz;
     }
-    float dx = p.dir[0], dy = p.dir[1], dz = p.dir[2];
+    float dx = f.dir[0], dy = f.dir[1], dz = f.dir[2];
     px = px - dx;
     py = py - dy;
     pz = pz - dz;
@@ -253,7 +214,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const rf_lens_element* 
         px = h.px;
         py = h.py;
         pz = h.pz;
-        if (lens_id == p.aperture) {
+        if (lens_id == f.aperture) {
             apt_x = h.px / e.height;
             apt_y = h.py / e.height;
             continue;
@@ -281,9 +242,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const rf_lens_element* 
             float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
             float reflectance;
             if (e.layers == 2) {
-                reflectance = fresnel_two_layer(theta, wavelength, n1, p.layer_n0, e.d0, p.layer_n1, e.d1, n2);
+                reflectance = fresnel_two_layer(theta, wavelength, n1, f.layer_n0, e.d0, f.layer_n1, e.d1, n2);
             } else if (e.layers == 1 || e.coating > 0) {
-                float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
+                float nc = fmaxf(sqrtf(n1 * n2), f.cmin);
                 float d1 = e.layers == 1 ? e.d0 : (float)e.coating / (4.0f * nc);
                 reflectance = fresnel_ar(theta, wavelength, d1, n1, nc, n2);
             } else {
@@ -304,13 +265,154 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const rf_lens_element* 
         }
     }
     if (lens_id >= 0 && lens_id < E) refl = __int_as_float(0x7fffffff);
+    out[0] = px;
+    out[1] = py;
+    out[2] = apt_x;
+    out[3] = apt_y;
+    out[4] = rrel;
+    out[5] = refl;
+}
+
+// Stage the lens elements and the refractive indices of wavelength rows [row0, row0 + span)
+// (row r = wavelength (row0 + r) % W) in shared memory; table false: too many rows.
+__device__ __forceinline__ void stage_lens(const rf_lens_element* __restrict__ elements, const float* __restrict__ wavelengths,
+                                           int E, int W, long long row0, int span, bool table, bool disperse,
+                                           SmemElement* se, float* ior_tab) {
+    for (int i = threadIdx.x; i < E; i += kTraceThreads) {
+        const rf_lens_element& e = elements[i];
+        se[i].radius = e.radius;
+        se[i].center = e.center;
+        se[i].height = e.height;
+        se[i].ior = e.ior;
+        se[i].coating = e.coating;
+        se[i].layers = e.coating_layers;
+        se[i].d0 = e.coating_thickness[0];
+        se[i].d1 = e.coating_thickness[1];
+    }
+    if (table) {
+        for (int k = threadIdx.x; k < span * E; k += kTraceThreads) {
+            int row = k / E, el = k % E;
+            int wl = (int)((row0 + row) % W);
+            float n = elements[el].ior;
+            if (disperse && n > 1.0f) n = dispersion(wavelengths[wl], elements[el].coefficients);
+            ior_tab[row * E + el] = n;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace(const rf_lens_element* __restrict__ elements,
+                                                         const int2* __restrict__ paths,
+                                                         const float* __restrict__ wavelengths,
+                                                         const __grid_constant__ TraceParams p,
+                                                         float* __restrict__ rays) {
+    __shared__ SmemElement se[kMaxElements];
+    __shared__ float ior_tab[kMaxTableWavelengths * kMaxElements];
+    const int E = p.E;
+    const long long first = (long long)blockIdx.x * kTraceThreads;
+    // wavelength rows this block needs: the span of (first, last) ray indices
+    const long long last = min(first + kTraceThreads, p.n_rays) - 1;
+    const long long pw_first = first / p.R, pw_last = last / p.R;
+    const long long span_rows = pw_last - pw_first + 1;
+    const int span = (int)(span_rows < (long long)p.W ? span_rows : (long long)p.W);
+    const bool table = span <= kMaxTableWavelengths;
+    // dispersion is on unless coefficient 0 of element 0 is NaN (raytracing.cl:255)
+    const bool disperse = !isnan(__ldg(&elements[0].coefficients[0]));
+    stage_lens(elements, wavelengths, E, p.W, pw_first, span, table, disperse, se, ior_tab);
+    __syncthreads();
+
+    const long long idx = first + threadIdx.x;
+    if (idx >= p.n_rays) return;
+    const int ray_id = (int)(idx % p.R);
+    const long long pw = idx / p.R;
+    const int wl_id = (int)(pw % p.W);
+    const int path_id = (int)(pw / p.W);
+    const int row = (int)((pw - pw_first) % p.W);
+    TraceFrame f;
+    f.E = E;
+    f.aperture = p.aperture;
+    f.W = p.W;
+    f.G = p.G;
+    f.R = p.R;
+    f.cmin = p.cmin;
+    f.layer_n0 = p.layer_n0;
+    f.layer_n1 = p.layer_n1;
+    f.dir[0] = p.dir[0];
+    f.dir[1] = p.dir[1];
+    f.dir[2] = p.dir[2];
+    // init_ray grid point, raytracing.cl:178-215
+    const int gy = (int)truncf((float)ray_id / (float)p.G);
+    const int gx = ray_id - gy * p.G;
+    float out[6];
+    trace_ray(se, table ? ior_tab + row * E : nullptr, disperse, &elements[0].coefficients[0],
+              __ldg(wavelengths + wl_id), __ldg(paths + path_id), p.grid[gx], p.grid[gy], f, out);
     const long long n = p.n_rays;
-    rays[idx] = px;
-    rays[n + idx] = py;
-    rays[2 * n + idx] = apt_x;
-    rays[3 * n + idx] = apt_y;
-    rays[4 * n + idx] = rrel;
-    rays[5 * n + idx] = refl;
+#pragma unroll
+    for (int k = 0; k < 6; k++) rays[k * n + idx] = out[k];
+}
+
+// Every frame of a batch: block b traces rays_per_thread * 256 consecutive rays of the frame
+// whose first trace block is the largest one <= b.
+__global__ void __launch_bounds__(kTraceThreads) k_trace_batch(const rf_frame* __restrict__ frames, int F,
+                                                               const rf_lens_element* __restrict__ elements_all,
+                                                               const int2* __restrict__ paths_all,
+                                                               const float* __restrict__ wavelengths_all,
+                                                               float* __restrict__ rays_all, int rays_per_thread) {
+    __shared__ SmemElement se[kMaxElements];
+    __shared__ float ior_tab[kMaxTableWavelengths * kMaxElements];
+    __shared__ float grid[kMaxGrid];
+    __shared__ int frame_index;
+    if (threadIdx.x == 0)
+        frame_index = find_frame(frames, F, blockIdx.x, [](const rf_frame& fr) { return fr.trace_block; });
+    __syncthreads();
+    const rf_frame& fr = frames[frame_index];
+    TraceFrame f;
+    f.E = fr.trace.element_count;
+    f.aperture = fr.trace.aperture_index;
+    f.W = fr.trace.wavelength_count;
+    f.G = fr.trace.grid_count;
+    f.R = f.G * f.G;
+    f.cmin = fr.trace.coating_min_ior;
+    f.layer_n0 = fr.trace.coating_layer_ior[0];
+    f.layer_n1 = fr.trace.coating_layer_ior[1];
+    f.dir[0] = fr.direction_n[0];
+    f.dir[1] = fr.direction_n[1];
+    f.dir[2] = fr.direction_n[2];
+    const long long n_rays = (long long)fr.trace.path_count * f.W * f.R;
+    const rf_lens_element* elements = elements_all + fr.element_offset;
+    const float* wavelengths = wavelengths_all + fr.wavelength_offset;
+    const int2* paths = paths_all + fr.path_offset;
+    float* rays = rays_all + 6 * fr.ray_offset;
+    const long long chunk = kTraceThreads * (long long)rays_per_thread;
+    const long long first = (blockIdx.x - fr.trace_block) * chunk;
+    const long long last = min(first + chunk, n_rays) - 1;
+    const long long pw_first = first / f.R, pw_last = last / f.R;
+    const long long span_rows = pw_last - pw_first + 1;
+    const int span = (int)(span_rows < (long long)f.W ? span_rows : (long long)f.W);
+    const bool table = span <= kMaxTableWavelengths;
+    const bool disperse = !isnan(__ldg(&elements[0].coefficients[0]));
+    stage_lens(elements, wavelengths, f.E, f.W, pw_first, span, table, disperse, se, ior_tab);
+    // grid_length * (x / (G - 1) - 0.5), in double as in the reference (and rf_trace's host table)
+    for (int i = threadIdx.x; i < f.G; i += kTraceThreads) {
+        const float t = (float)i / (float)(f.G - 1);
+        grid[i] = (float)((double)fr.trace.grid_length * ((double)t - 0.5));
+    }
+    __syncthreads();
+    for (int r = 0; r < rays_per_thread; r++) {
+        const long long idx = first + r * kTraceThreads + threadIdx.x;
+        if (idx > last) break;
+        const int ray_id = (int)(idx % f.R);
+        const long long pw = idx / f.R;
+        const int wl_id = (int)(pw % f.W);
+        const int path_id = (int)(pw / f.W);
+        const int row = (int)((pw - pw_first) % f.W);
+        const int gy = (int)truncf((float)ray_id / (float)f.G);
+        const int gx = ray_id - gy * f.G;
+        float out[6];
+        trace_ray(se, table ? ior_tab + row * f.E : nullptr, disperse, &elements[0].coefficients[0],
+                  __ldg(wavelengths + wl_id), __ldg(paths + path_id), grid[gx], grid[gy], f, out);
+#pragma unroll
+        for (int k = 0; k < 6; k++) rays[k * n_rays + idx] = out[k];
+    }
 }
 
 }  // namespace
@@ -350,5 +452,16 @@ extern "C" int rf_trace(const rf_lens_element* elements, const int32_t* paths, c
     }
     k_trace<<<blocks_for(p.n_rays, kTraceThreads), kTraceThreads, 0, (cudaStream_t)stream>>>(
         elements, (const int2*)paths, wavelengths, p, rays);
+    return launch_status();
+}
+
+extern "C" int rf_trace_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const rf_lens_element* elements,
+                              const int32_t* paths, const float* wavelengths, float* rays, void* stream) {
+    using namespace rf;
+    if (!frames || !sizes || !elements || !paths || !wavelengths || !rays) return RF_ERR_INVALID_ARG;
+    if (sizes->trace_blocks == 0) return RF_OK;
+    if (sizes->trace_blocks > 0x7fffffffLL) return RF_ERR_NOT_SUPPORTED;
+    k_trace_batch<<<(unsigned)sizes->trace_blocks, kTraceThreads, 0, (cudaStream_t)stream>>>(
+        frames, sizes->frame_count, elements, (const int2*)paths, wavelengths, rays, sizes->rays_per_thread);
     return launch_status();
 }

@@ -185,3 +185,31 @@ def workload(name: str, integer_wavelengths: bool = False) -> Workload:
     paths = lens_mod.all_two_bounce_paths(model)
     p.flare.lens.ghost_paths = tuple(tuple(pp) for pp in paths)
     return Workload(name, p, paths)
+
+
+BATCH_SURFACES = (8, 16, 24)
+BATCH_GRIDS = (32, 64, 128)
+
+
+def batched_projects(count: int = 256, seed: int = 0, resolution: int = 1024, surfaces: tuple = BATCH_SURFACES,
+                     grids: tuple = BATCH_GRIDS, max_wavelengths: int = 16) -> list:
+    """Frame requests of the batched form: per request a lens drawn from the 8-, 16- and
+    24-surface workload lenses (all their two-bounce ghosts: 28 / 120 / 276), a grid of
+    32^2, 64^2 or 128^2, 1-16 wavelengths spread over 390-700 nm (550 nm for one) and a
+    light position uniform over the normalised field, rendered at resolution^2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    names = {8: 'plain-8', 16: 'spectral-16', 24: 'production-24'}
+    lenses = {n: workload(names[n]) for n in surfaces}
+    projects = []
+    for _ in range(count):
+        n = int(rng.choice(np.array(surfaces)))
+        grid = int(rng.choice(np.array(grids)))
+        w = int(rng.integers(1, max_wavelengths + 1))
+        light = rng.uniform(-1.0, 1.0, 2)
+        base = lenses[n].project
+        wl = [550.0] if w == 1 else list(np.linspace(390.0, 700.0, w))
+        p = _project(base.flare.lens.lens_model, grid, wl, (float(light[0]), float(light[1])), resolution,
+                     base.flare.lens.coating, base.flare.lens.coating_thickness)
+        p.flare.lens.ghost_paths = base.flare.lens.ghost_paths
+        projects.append(p)
+    return projects

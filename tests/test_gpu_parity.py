@@ -138,12 +138,14 @@ def gpu_tiles(ra, bounds_d, vtx_d):
     return offsets, entries, task
 
 
+@pytest.mark.parametrize('tile', [32, 16])
 @pytest.mark.parametrize('key', list(WORKLOADS))
-def test_tile_lists_ordered_and_within_reference_bins(oracle, key):
+def test_tile_lists_ordered_and_within_reference_bins(oracle, key, tile):
     w = workload(key)
     ghost = ghost_texture()
     r = oracle_pipeline(oracle, w, ghost, light_spectrum())
     ra = r['raster_args']
+    ra.tile_size = tile
     offsets, entries, task = gpu_tiles(ra, dev(r['bounds']), dev(r['vtx']))
     T = task.tile_size
     off = offsets.cpu().numpy().astype(np.int64)
@@ -167,13 +169,15 @@ def test_tile_lists_ordered_and_within_reference_bins(oracle, key):
         assert np.all((words >> (bits % 64).astype(np.uint64)) & np.uint64(1)), 'entry outside its reference bin'
 
 
+@pytest.mark.parametrize('tile', [32, 16])
 @pytest.mark.parametrize('key', list(WORKLOADS))
-def test_raster_matches_oracle(oracle, key):
+def test_raster_matches_oracle(oracle, key, tile):
     w = workload(key)
     ghost = ghost_texture()
     spec = light_spectrum()
     r = oracle_pipeline(oracle, w, ghost, spec)
     ra = r['raster_args']
+    ra.tile_size = tile
     bounds_d, vtx_d = dev(r['bounds']), dev(r['vtx'])
     offsets, entries, task = gpu_tiles(ra, bounds_d, vtx_d)
     image = torch.empty((ra.height, ra.width, 4), device='cuda')
