@@ -49,6 +49,8 @@ def parse_args():
     # reductions of the workload for profiler captures (recorded in the line's config)
     ap.add_argument('--image', type=int, default=0, help='square image size override')
     ap.add_argument('--ghosts', type=int, default=0, help='keep only the first N ghosts')
+    ap.add_argument('--batched-frames', type=int, default=256,
+                    help='frames of the batched form measured beside the plain path (0 = skip)')
     ap.add_argument('--raster-stats', action='store_true',
                     help='count k_raster work (statistics build of the library) instead of timing')
     return ap.parse_args()
@@ -528,6 +530,7 @@ def main() -> None:
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(w, args)
+    batched = run_batched(args) if args.batched_frames > 0 and rank == 0 else None
 
     peak, peak_kind = load_peaks()
     raster_s = last['raster'] / 1e3
@@ -576,6 +579,7 @@ def main() -> None:
             'cpu_baseline': cpu,
             'clocks': clk,
             'gpu_launches': launches,
+            'batched': batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -622,6 +626,79 @@ def run_raster_stats(args) -> None:
         },
         'config': {'workload': args.workload, 'image': f'{wd}x{h}', 'ghosts': frame.P},
     }), flush=True)
+
+
+def run_batched(args) -> dict:
+    """The batched form against per-frame plain launches on the same frames: 256 requests
+    (lenses with 8/16/24 surfaces, 32^2/64^2/128^2 grids, 1-16 wavelengths, lights uniform
+    over the field) at 1024^2. Frames are grouped under a device-memory budget; each group
+    is one launch per stage, captured as one CUDA graph and replayed (timed). The plain
+    path renders frame by frame through the task API (trace, setup, bin with its host
+    synchronisation, raster). Both are timed from a synchronised start to a synchronised
+    end; the images are compared bit for bit."""
+    import numpy as np
+    import torch
+
+    from realflare_gb300 import synthetic
+    from realflare_gb300.autotune import autotune
+    from realflare_gb300.batch import BatchRenderer, ghost_textures, group_frames
+    from realflare_gb300.device import Image
+    from realflare_gb300.tasks import RasterizingTask, RaytracingTask
+
+    n = args.batched_frames
+    projects = synthetic.batched_projects(n, seed=0, resolution=1024)
+    ghosts = ghost_textures(projects)
+    tex, offsets, shapes = ghosts
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(min(0.3 * free, 60e9))
+    groups = group_frames(projects, budget)
+    # autotune on a sample spread over the batch (the knobs do not change the images)
+    sample = projects[:: max(1, n // 24)][:24]
+    choice = autotune(sample)
+
+    # batched: per group build, size and capture (untimed), then time the graph replays
+    batched_s, sums_batched = 0.0, []
+    for g in groups:
+        r = BatchRenderer([projects[i] for i in g], tile_size=choice.tile_size,
+                          rays_per_thread=choice.rays_per_thread, ghosts=(tex, [offsets[i] for i in g],
+                                                                         [shapes[i] for i in g]))
+        r.run()
+        r.capture()
+        r.replay()  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.replay()
+        torch.cuda.synchronize()
+        batched_s += time.perf_counter() - t0
+        sums_batched += [float(im.double().sum()) for im in r.images]
+        del r
+    # plain: frame after frame through the task API
+    trace, raster = RaytracingTask(cache=False), RasterizingTask()
+    for p in projects[:2]:  # warm-up
+        raster.run(p, trace.run(p), Image(tensor=tex[offsets[0]: offsets[0] + shapes[0][0] * shapes[0][1]]
+                                          .view(*shapes[0])))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    images = []
+    for i, p in enumerate(projects):
+        h, w = shapes[i]
+        img = raster.run(p, trace.run(p), Image(tensor=tex[offsets[i]: offsets[i] + h * w].view(h, w)))
+        images.append(img.tensor.double().sum())
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    sums_plain = [float(x) for x in images]
+    identical = bool(np.array_equal(np.array(sums_batched), np.array(sums_plain)))
+    rays = sum(p.render.grid_count ** 2 * p.render.wavelength_count * len(p.flare.lens.ghost_paths)
+               for p in projects)
+    return {
+        'frames': n, 'image': '1024x1024', 'rays': rays,
+        'frames_per_s': n / batched_s, 'plain_frames_per_s': n / plain_s, 'speedup_vs_plain': plain_s / batched_s,
+        'groups': len(groups), 'memory_budget_gb': round(budget / 1e9, 1),
+        'tile_size': choice.tile_size, 'rays_per_thread': choice.rays_per_thread,
+        'autotune_ms': {k: round(v, 3) for k, v in choice.timings_ms.items()},
+        'identical_to_plain': identical,
+        'timing': 'wall clock from a synchronised start to a synchronised end; batched = CUDA-graph replays',
+    }
 
 
 def run_e2e(w, args) -> dict:
