@@ -317,6 +317,43 @@ int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const f
                     const float* spectrum, void* workspace, size_t workspace_bytes,
                     int64_t entry_capacity, const uint64_t* entry_total, float* images, void* stream);
 
+/* ---- differentiation ------------------------------------------------------------------- */
+/* Adjoint (reverse-mode derivative) of rf_trace; no reference counterpart (the reference
+ * has no derivatives). grad_rays: device float[RF_RAY_PLANES][n_rays], the gradient of a
+ * loss with respect to rf_trace's outputs (sensor x, y; aperture x, y; rrel; reflectance).
+ * Writes grad_elements: device float[element_count][4], the gradient with respect to each
+ * element's radius, center, coating_thickness[0] and coating_thickness[1], and
+ * grad_direction: device float[3], with respect to normalize(-direction.xyz). Rays that do
+ * not reach the sensor contribute nothing; each ray's discrete choices (elements hit,
+ * reflections, the element giving rrel) are held fixed. element_count <= 32. */
+int rf_trace_adjoint(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
+                     const rf_trace_args* args, const float* grad_rays, float* grad_elements,
+                     float* grad_direction, void* stream);
+
+/* Adjoint of rf_raster (32 x 32 tiles; the same tile lists). Coverage and the mean-value
+ * weights depend on the vertex positions only through integer sample coordinates, so they
+ * are held fixed: the gradient flows to each vertex's interpolated attributes (aperture
+ * position, rrel, reflectance, intensity), not to its screen position (the change of
+ * covered pixels as quad edges move is not included). image: rf_raster's output; grad_image:
+ * device float[height][width][4]; grad_vertexes: device float[n_vertices][8] (the vertex
+ * layout; floats 2..6 receive the gradients), zeroed by this call. */
+int rf_raster_backward(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                       const float* ghost, const float* spectrum, const rf_raster_args* args,
+                       const float* image, const float* grad_image, float* grad_vertexes, void* stream);
+
+/* Adjoint of rf_vertex: writes grad_rays planes 2..5 (aperture x, y, rrel, reflectance)
+ * from grad_vertexes, zeroes planes 0..1, and writes grad_intensities (device
+ * float[path_count][quads][wavelength_count]) from the vertices' averaged intensities. */
+int rf_vertex_backward(const float* rays, const float* intensities, int32_t path_count,
+                       int32_t wavelength_count, int32_t grid_count, const float* grad_vertexes,
+                       float* grad_rays, float* grad_intensities, void* stream);
+
+/* Adjoint of rf_quad_setup's intensity area_orig / max(area, min_area): adds the gradient
+ * of the quads' sensor-plane areas to grad_rays planes 0..1 (sensor x, y). */
+int rf_quad_setup_backward(const float* rays, int32_t path_count, int32_t wavelength_count,
+                           int32_t grid_count, float area_orig, float min_area,
+                           const float* grad_intensities, float* grad_rays, void* stream);
+
 /* ---- compositing ---------------------------------------------------------------------- */
 /* out = a * wa + b * wb elementwise over n floats (Engine.flare_starburst,
  * realflare/api/engine.py:174-187, uses wa = 2, wb = 1). */

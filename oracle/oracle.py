@@ -45,6 +45,7 @@ class Oracle:
             lib = ctypes.CDLL(build_oracle.lib_path(variant))
             lib.rfo_trace.argtypes = [_P, _P, _P, ctypes.POINTER(TraceArgs), _P]
             lib.rfo_trace_range.argtypes = [_P, _P, _P, ctypes.POINTER(TraceArgs), _P, _LL, _LL]
+            lib.rfo_trace_d.argtypes = [_P, _P, _P, ctypes.POINTER(TraceArgs), _P]
             lib.rfo_quad_setup.argtypes = [_P, _I, _I, _I, _F, _F, _P, _P]
             lib.rfo_vertex.argtypes = [_P, _P, _I, _I, _I, _F, _I, _I, _P]
             lib.rfo_bin_masks.argtypes = [_P, _I, _F, _I, _I, _I, _P]
@@ -68,6 +69,15 @@ class Oracle:
             self.lib.rfo_trace(_ptr(el), _ptr(pa), _ptr(wl), ctypes.byref(args), _ptr(out))
         else:
             self.lib.rfo_trace_range(_ptr(el), _ptr(pa), _ptr(wl), ctypes.byref(args), _ptr(out), first, count)
+        return out
+
+    def trace_d(self, elements, paths, wavelengths, args: TraceArgs):
+        """trace() with the outputs in double (for finite differences of the FP64 build)."""
+        n = args.path_count * args.wavelength_count * args.grid_count**2
+        out = np.zeros((6, n), np.float64)
+        el = _c(elements, elements.dtype)
+        self.lib.rfo_trace_d(_ptr(el), _ptr(_c(paths, np.int32)), _ptr(_c(wavelengths, np.float32)),
+                             ctypes.byref(args), _ptr(out))
         return out
 
     def quad_setup(self, rays, P, W, G, area_orig, min_area):

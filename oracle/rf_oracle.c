@@ -155,11 +155,10 @@ static real dispersion(real lambda, const float* c) {
 
 typedef struct { v3 pos, normal; real incident; int hit; } hit_t;
 
-/* intersect, raytracing.cl:123-175 */
-static hit_t intersect(v3 pos, v3 dir, const rf_lens_element* e) {
+/* intersect, raytracing.cl:123-175, with the element's radius and center given */
+static hit_t intersect_rc(v3 pos, v3 dir, real radius, real center) {
     hit_t h;
     memset(&h, 0, sizeof(h));
-    real radius = (real)e->radius, center = (real)e->center;
     if (dir.z == 0) {
         h.hit = 0;
     } else if (radius == 0) {
@@ -191,6 +190,10 @@ static hit_t intersect(v3 pos, v3 dir, const rf_lens_element* e) {
     return h;
 }
 
+static hit_t intersect(v3 pos, v3 dir, const rf_lens_element* e) {
+    return intersect_rc(pos, dir, (real)e->radius, (real)e->center);
+}
+
 /* reflect / refract, raytracing.cl:70-102 */
 static v3 reflect3(v3 i, v3 n) { return add3(i, mul3(n, K(2) * dot3(n, neg3(i)))); }
 static v3 refract3(v3 i, v3 n, real o) {
@@ -211,8 +214,12 @@ static void grid_point(int ray_id, int grid_count, real grid_length, real* px, r
 }
 
 /* raytrace kernel, raytracing.cl:178-359. rays: RF_RAY_PLANES planes of P*W*R floats. */
+/* geom (optional, finite-difference checks): per element radius, center, coating
+ * thickness 0 and 1 in double, replacing the element's float fields; dir3 (optional): the
+ * light direction in double. */
 static void trace_one(const rf_lens_element* el, const int32_t* paths, const float* wavelengths,
-                      const rf_trace_args* a, size_t idx, float* rays, size_t n_rays) {
+                      const rf_trace_args* a, size_t idx, float* rays, double* rays_d, size_t n_rays,
+                      const double* geom, const double* dir3) {
     const int E = a->element_count;
     const int R = a->grid_count * a->grid_count;
     const int ray_id = (int)(idx % (size_t)R);
@@ -224,9 +231,14 @@ static void trace_one(const rf_lens_element* el, const int32_t* paths, const flo
     real gx, gy;
     grid_point(ray_id, a->grid_count, (real)a->grid_length, &gx, &gy);
     v3 pos = mk3(gx, gy, 1), dir = mk3(0, 0, -1);
-    hit_t h0 = intersect(pos, dir, &el[0]);
+#define RFO_RADIUS(i) (geom ? (real)geom[4 * (i)] : (real)el[i].radius)
+#define RFO_CENTER(i) (geom ? (real)geom[4 * (i) + 1] : (real)el[i].center)
+#define RFO_T0(i) (geom ? (real)geom[4 * (i) + 2] : (real)el[i].coating_thickness[0])
+#define RFO_T1(i) (geom ? (real)geom[4 * (i) + 3] : (real)el[i].coating_thickness[1])
+    hit_t h0 = intersect_rc(pos, dir, RFO_RADIUS(0), RFO_CENTER(0));
     pos = h0.pos; /* zero when the grid point misses element 0 */
-    v3 direction = norm3(neg3(mk3((real)a->direction[0], (real)a->direction[1], (real)a->direction[2])));
+    v3 direction = dir3 ? norm3(neg3(mk3((real)dir3[0], (real)dir3[1], (real)dir3[2])))
+                        : norm3(neg3(mk3((real)a->direction[0], (real)a->direction[1], (real)a->direction[2])));
     pos = sub3(pos, direction);
     dir = direction;
     real apt_x = 0, apt_y = 0, rrel = 0, refl = 1;
@@ -236,7 +248,7 @@ static void trace_one(const rf_lens_element* el, const int32_t* paths, const flo
     int lens_id;
     for (lens_id = 0; lens_id >= 0 && lens_id < E; lens_id += delta) {
         const rf_lens_element* e = &el[lens_id];
-        hit_t h = intersect(pos, dir, e);
+        hit_t h = intersect_rc(pos, dir, RFO_RADIUS(lens_id), RFO_CENTER(lens_id));
         if (!h.hit) break;
         pos = h.pos;
         if (lens_id == a->aperture_index) {
@@ -264,13 +276,11 @@ static void trace_one(const rf_lens_element* el, const int32_t* paths, const flo
             real reflectance;
             if (e->coating_layers == 2) {
                 reflectance = fresnel_two_layer(theta, wavelength, n1, (real)a->coating_layer_ior[0],
-                                                (real)e->coating_thickness[0],
-                                                (real)a->coating_layer_ior[1],
-                                                (real)e->coating_thickness[1], n2);
+                                                RFO_T0(lens_id), (real)a->coating_layer_ior[1],
+                                                RFO_T1(lens_id), n2);
             } else if (e->coating_layers == 1 || e->coating > 0) {
                 real nc = rmax(sqrt(n1 * n2), (real)a->coating_min_ior);
-                real d1 = e->coating_layers == 1 ? (real)e->coating_thickness[0]
-                                                 : (real)e->coating / (K(4) * nc);
+                real d1 = e->coating_layers == 1 ? RFO_T0(lens_id) : (real)e->coating / (K(4) * nc);
                 reflectance = fresnel_ar(theta, wavelength, d1, n1, nc, n2);
             } else {
                 reflectance = fresnel(theta, n1, n2);
@@ -282,7 +292,20 @@ static void trace_one(const rf_lens_element* el, const int32_t* paths, const flo
             if (dir.z == 0) break;
         }
     }
+#undef RFO_RADIUS
+#undef RFO_CENTER
+#undef RFO_T0
+#undef RFO_T1
     if (lens_id >= 0 && lens_id < E) refl = (real)NAN;
+    if (rays_d) { /* unrounded outputs (finite-difference checks of the FP64 build) */
+        rays_d[0 * n_rays + idx] = (double)pos.x;
+        rays_d[1 * n_rays + idx] = (double)pos.y;
+        rays_d[2 * n_rays + idx] = (double)apt_x;
+        rays_d[3 * n_rays + idx] = (double)apt_y;
+        rays_d[4 * n_rays + idx] = (double)rrel;
+        rays_d[5 * n_rays + idx] = (double)refl;
+        return;
+    }
     rays[0 * n_rays + idx] = (float)pos.x;
     rays[1 * n_rays + idx] = (float)pos.y;
     rays[2 * n_rays + idx] = (float)apt_x;
@@ -296,7 +319,28 @@ int rfo_trace(const rf_lens_element* el, const int32_t* paths, const float* wave
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, n);
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL);
+    return 0;
+}
+
+/* rfo_trace with the element geometry (radius, center, coating thicknesses per element) and
+ * the light direction given in double, outputs in double (finite-difference checks). */
+int rfo_trace_geom_d(const rf_lens_element* el, const int32_t* paths, const float* wavelengths,
+                     const rf_trace_args* a, const double* geom, const double* dir3, double* rays) {
+    const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
+    const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, geom, dir3);
+    return 0;
+}
+
+/* rfo_trace with outputs in double, not rounded to float. */
+int rfo_trace_d(const rf_lens_element* el, const int32_t* paths, const float* wavelengths,
+                const rf_trace_args* a, double* rays) {
+    const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
+    const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, NULL, NULL);
     return 0;
 }
 
@@ -306,7 +350,7 @@ int rfo_trace_range(const rf_lens_element* el, const int32_t* paths, const float
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = first; i < first + count; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, n);
+    for (long long i = first; i < first + count; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL);
     return 0;
 }
 
@@ -673,6 +717,73 @@ static void finish_pixel(const rf_raster_args* a, int x, int y, const real rgb[3
         float* out = image + 4 * ((size_t)(a->height - (y + 1)) * a->width + x);
         xyz_to_ap1(v, out);
     }
+}
+
+/* Fragments (covered pixel x primitive x wavelength pair x sub-wavelength) of the
+ * rasterizer, in its loop order, with their hit counts and mean-value weights: the frozen
+ * coverage of finite-difference checks of the render's derivative. Writes at most capacity
+ * fragments: pixel index y * width + x (unflipped), primitive, pair, sub-wavelength, hits and
+ * 4 weights; returns the count. */
+long long rfo_raster_fragments(const float* vertexes, const uint64_t* masks, int batch_count,
+                               const rf_raster_args* a, long long capacity, int32_t* pixel, int64_t* prim_out,
+                               int32_t* pair, int32_t* sub, int32_t* hits_out, double* weights) {
+    const int B = a->bin_size;
+    const int bdx = (a->width + B - 1) / B;
+    const int G = a->grid_count, W = a->wavelength_count, WS = a->wavelength_sub_count, S = a->sub_steps;
+    const int Q = (G - 1) * (G - 1), VC = G * G;
+    const int maxW = W - 1 > 1 ? W - 1 : 1;
+    const long long prim_total = (long long)a->path_count * Q;
+    long long count = 0;
+    for (int y = 0; y < a->height; y++) {
+        for (int x = 0; x < a->width; x++) {
+            int bin = (y / B) * bdx + (x / B);
+            const int32_t ppx = x * S, ppy = y * S, pcx = ppx + S / 2, pcy = ppy + S / 2;
+            for (int batch = 0; batch < batch_count; batch++) {
+                const uint64_t* q = masks + 4 * ((size_t)bin * batch_count + batch);
+                if ((q[0] & 1u) == 0) continue;
+                for (int k = 0; k < RF_BATCH_PRIMITIVE_COUNT; k++) {
+                    long long prim = (long long)batch * RF_BATCH_PRIMITIVE_COUNT + k;
+                    if (prim >= prim_total) continue;
+                    int bit = k + 1;
+                    if (!((q[bit >> 6] >> (bit & 63)) & 1u)) continue;
+                    long long path = prim / Q;
+                    int quad = (int)(prim % Q), row = quad / (G - 1), col = quad % (G - 1);
+                    long long vq[4] = {row * G + col, row * G + col + 1, row * G + col + 1 + G, row * G + col + G};
+                    for (int w = 0; w < maxW; w++) {
+                        real sub_pos = 0;
+                        const real sub_step = K(1) / (real)WS;
+                        for (int i = 0; i < WS; i++) {
+                            int32_t qq[8];
+                            for (int j = 0; j < 4; j++) {
+                                const float* s0 = vertexes + 8 * ((path * VC + vq[j]) * W + w);
+                                const float* s1 = s0 + 8;
+                                qq[2 * j] = cvt_rz_sat(mixr((real)s0[0], (real)s1[0], sub_pos) * (real)S);
+                                qq[2 * j + 1] = cvt_rz_sat(mixr((real)s0[1], (real)s1[1], sub_pos) * (real)S);
+                            }
+                            int hits = 0;
+                            for (int s = 0; s < S; s++)
+                                if (intersect_quad(ppx + s, ppy + SUB_OFFSETS[S - 1 + s], qq)) hits++;
+                            if (hits > 0) {
+                                if (count < capacity) {
+                                    real wt[4];
+                                    barycentric_quad(pcx, pcy, qq, wt);
+                                    pixel[count] = y * a->width + x;
+                                    prim_out[count] = prim;
+                                    pair[count] = w;
+                                    sub[count] = i;
+                                    hits_out[count] = hits;
+                                    for (int j = 0; j < 4; j++) weights[4 * count + j] = (double)wt[j];
+                                }
+                                count++;
+                            }
+                            sub_pos += sub_step;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return count;
 }
 
 /* rasterizer kernel over the reference's bin masks, rasterizing.cl:524-663 */

@@ -161,6 +161,10 @@ SIGNATURES = {
     'rf_aperture_dust': [P, I32, I32, F32, F32, F32, F32, F32, F32, F32, F32, P],
     'rf_aperture_noise_dust': [P, P, P, I32, I32, F32, F32, P],
     'rf_axpby': [P, F32, P, F32, P, I64, P],
+    'rf_trace_adjoint': [P, P, P, ctypes.POINTER(TraceArgs), P, P, P, P],
+    'rf_raster_backward': [P, P, P, P, P, ctypes.POINTER(RasterArgs), P, P, P, P],
+    'rf_vertex_backward': [P, P, I32, I32, I32, P, P, P, P],
+    'rf_quad_setup_backward': [P, I32, I32, I32, F32, F32, P, P, P],
     'rf_batch_plan': [ctypes.POINTER(Frame), I32, I32, I32, ctypes.POINTER(BatchSizes)],
     'rf_trace_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P, P],
     'rf_quad_setup_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P],

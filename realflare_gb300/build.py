@@ -32,6 +32,8 @@ UNITS = {
     'rf_fft.cu': [],
     'rf_image.cu': [],
     'rf_batch.cu': [],
+    # the adjoint re-traces rays: it must use the trace's arithmetic
+    'rf_adjoint.cu': [] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false'],
 }
 
 

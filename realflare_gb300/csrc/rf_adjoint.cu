@@ -1,0 +1,454 @@
+// rf_adjoint.cu — reverse-mode derivative (adjoint) of the ghost ray trace.
+//
+// No reference counterpart: the reference has no differentiation. Given the gradient of a
+// loss with respect to every traced ray's outputs (sensor position, aperture position,
+// rrel, reflectance), rf_trace_adjoint returns the gradient with respect to every lens
+// element's radius, center and coating thicknesses and to the (normalised) light direction.
+//
+// Per ray, the thread re-traces the ray with the forward's own code (rf_trace_core.cuh,
+// compiled like rf_trace.cu without floating-point contraction, so the re-trace takes the
+// same path), recording the position and direction entering each element; the surfaces
+// (hit point, normal) are recomputed from those in the reverse sweep instead of being
+// stored. The reverse sweep applies, element by element from the sensor back to the entry,
+// the transposed Jacobians of intersect (sphere or plane), refract, reflect and the coating
+// reflectance (the last by three-tangent forward-mode duals of the Fresnel formulas), then
+// the entry ray (grid point hitting element 0, stepped back along the light direction).
+// Rays that do not reach the sensor have no outputs and no gradient; the discrete choices
+// (which element is hit, reflection or refraction, the rrel maximum) are those of the
+// forward, i.e. the gradient is the derivative wherever they do not change.
+#include "rf_trace_core.cuh"
+
+namespace rf {
+namespace {
+
+constexpr int kAdjThreads = 128;
+constexpr int kAdjMaxElements = 32;
+constexpr int kAdjMaxSteps = 3 * kAdjMaxElements;
+constexpr int kAdjTableRows = 4;
+constexpr int kGradPerElement = 4;  // radius, center, coating thickness 0 and 1
+
+// ---------------------------------------------------------------- three-tangent duals
+struct D3 {
+    float v, g0, g1, g2;
+};
+__device__ __forceinline__ D3 dconst(float v) { return {v, 0.f, 0.f, 0.f}; }
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return {a.v + b.v, a.g0 + b.g0, a.g1 + b.g1, a.g2 + b.g2}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return {a.v - b.v, a.g0 - b.g0, a.g1 - b.g1, a.g2 - b.g2}; }
+__device__ __forceinline__ D3 operator-(D3 a) { return {-a.v, -a.g0, -a.g1, -a.g2}; }
+__device__ __forceinline__ D3 operator*(D3 a, D3 b) {
+    return {a.v * b.v, a.g0 * b.v + a.v * b.g0, a.g1 * b.v + a.v * b.g1, a.g2 * b.v + a.v * b.g2};
+}
+__device__ __forceinline__ D3 operator*(D3 a, float s) { return {a.v * s, a.g0 * s, a.g1 * s, a.g2 * s}; }
+__device__ __forceinline__ D3 operator*(float s, D3 a) { return a * s; }
+__device__ __forceinline__ D3 operator/(D3 a, D3 b) {
+    const float q = a.v / b.v, ib = 1.0f / b.v;
+    return {q, (a.g0 - q * b.g0) * ib, (a.g1 - q * b.g1) * ib, (a.g2 - q * b.g2) * ib};
+}
+__device__ __forceinline__ D3 operator/(D3 a, float s) { return a * (1.0f / s); }
+__device__ __forceinline__ D3 chain(float v, float dv, D3 a) { return {v, dv * a.g0, dv * a.g1, dv * a.g2}; }
+__device__ __forceinline__ D3 dsin(D3 a) { return chain(sinf(a.v), cosf(a.v), a); }
+__device__ __forceinline__ D3 dcos(D3 a) { return chain(cosf(a.v), -sinf(a.v), a); }
+__device__ __forceinline__ D3 dtan(D3 a) {
+    const float t = tanf(a.v);
+    return chain(t, 1.0f + t * t, a);
+}
+__device__ __forceinline__ D3 dasin(D3 a) { return chain(asinf(a.v), rsqrtf(fmaxf(1.0f - a.v * a.v, 1e-30f)), a); }
+__device__ __forceinline__ D3 dsqrt(D3 a) {
+    const float r = sqrtf(a.v);
+    return chain(r, r > 0.0f ? 0.5f / r : 0.0f, a);
+}
+
+// the Fresnel formulas of rf_trace_core.cuh over duals (theta in tangent 0, the coating
+// thicknesses in tangents 1 and 2)
+__device__ D3 fresnel_d(D3 theta0, float n1, float n2) {
+    D3 theta1 = dasin(dsin(theta0) * n1 / n2);
+    D3 cosi = dcos(theta0), cost = dcos(theta1);
+    D3 rs = (cosi * n1 - cost * n2) / (cosi * n1 + cost * n2);
+    D3 rp = (cost * n1 - cosi * n2) / (cost * n1 + cosi * n2);
+    return (rs * rs + rp * rp) / 2.0f;
+}
+__device__ D3 fresnel_ar_d(D3 theta0, float lambda, D3 d1, float n0, float n1, float n2) {
+    D3 s0 = dsin(theta0);
+    D3 theta1 = dasin(s0 * n0 / n1);
+    D3 theta2 = dasin(s0 * n0 / n2);
+    D3 rs01 = -dsin(theta0 - theta1) / dsin(theta0 + theta1);
+    D3 rp01 = dtan(theta0 - theta1) / dtan(theta0 + theta1);
+    D3 ts01 = 2.0f * dsin(theta1) * dcos(theta0) / dsin(theta0 + theta1);
+    D3 tp01 = ts01 * dcos(theta0 - theta1);
+    D3 rs12 = -dsin(theta1 - theta2) / dsin(theta1 + theta2);
+    D3 rp12 = dtan(theta1 - theta2) / dtan(theta1 + theta2);
+    D3 ris = ts01 * ts01 * rs12;
+    D3 rip = tp01 * tp01 * rp12;
+    D3 dy = d1 * n1;
+    D3 dx = dtan(theta1) * dy;
+    D3 delay = dsqrt(dx * dx + dy * dy);
+    D3 rel_phase = (delay - dx * s0) * (4.0f * RF_MPI_F / lambda);
+    D3 c = dcos(rel_phase);
+    D3 out_s2 = rs01 * rs01 + ris * ris + 2.0f * rs01 * ris * c;
+    D3 out_p2 = rp01 * rp01 + rip * rip + 2.0f * rp01 * rip * c;
+    return (out_s2 + out_p2) / 2.0f;
+}
+__device__ void interface_r_d(float ni, D3 ci, float nj, D3 cj, D3& rs, D3& rp) {
+    rs = (ci * ni - cj * nj) / (ci * ni + cj * nj);
+    rp = (ci * nj - cj * ni) / (ci * nj + cj * ni);
+}
+__device__ D3 stack_r2_d(D3 r01, D3 r12, D3 r23, D3 d1, D3 d2) {
+    D3 s2 = dsin(d2), c2 = dcos(d2), s1 = dsin(d1), c1 = dcos(d1);
+    D3 nre = r12 + r23 * c2, nim = r23 * s2;
+    D3 dre = dconst(1.0f) + r12 * r23 * c2, dim = r12 * r23 * s2;
+    D3 den = dre * dre + dim * dim;
+    D3 ire = (nre * dre + nim * dim) / den;
+    D3 iim = (nim * dre - nre * dim) / den;
+    D3 ere = ire * c1 - iim * s1, eim = ire * s1 + iim * c1;
+    D3 tre = r01 + ere, tim = eim;
+    D3 bre = dconst(1.0f) + r01 * ere, bim = r01 * eim;
+    return (tre * tre + tim * tim) / (bre * bre + bim * bim);
+}
+__device__ D3 fresnel_two_layer_d(D3 theta0, float lambda, float n0, float na, D3 da, float nb, D3 db, float n2) {
+    D3 s0 = dsin(theta0), c0 = dcos(theta0);
+    D3 sa = s0 * (n0 / na), sb = s0 * (n0 / nb), s2 = s0 * (n0 / n2);
+    D3 ca = dsqrt(dconst(1.0f) - sa * sa), cb = dsqrt(dconst(1.0f) - sb * sb), c2 = dsqrt(dconst(1.0f) - s2 * s2);
+    D3 rs01, rp01, rs12, rp12, rs23, rp23;
+    interface_r_d(n0, c0, na, ca, rs01, rp01);
+    interface_r_d(na, ca, nb, cb, rs12, rp12);
+    interface_r_d(nb, cb, n2, c2, rs23, rp23);
+    const float phase = 4.0f * RF_MPI_F / lambda;
+    D3 d1 = da * ca * (phase * na);
+    D3 d2 = db * cb * (phase * nb);
+    return (stack_r2_d(rs01, rs12, rs23, d1, d2) + stack_r2_d(rp01, rp12, rp23, d1, d2)) / 2.0f;
+}
+
+// ---------------------------------------------------------------- recording
+struct Step {
+    float px, py, pz, dx, dy, dz;
+    int lens;
+    int reflect;  // 1 when the ray reflects at this element
+};
+struct StepRecorder {
+    Step* steps;
+    int n;
+    int argmax;  // step whose |xy| / height is the final rrel
+    float best;
+    __device__ __forceinline__ void step(int lens, float px, float py, float pz, float dx, float dy, float dz) {
+        if (n < kAdjMaxSteps) steps[n] = {px, py, pz, dx, dy, dz, lens, 0};
+        n++;
+    }
+    __device__ __forceinline__ void rrel(float r, float) {
+        if (r > best) {
+            best = r;
+            argmax = n - 1;
+        }
+    }
+    __device__ __forceinline__ void reflect() {
+        if (n - 1 < kAdjMaxSteps) steps[n - 1].reflect = 1;
+    }
+};
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Reverse of intersect(p, d, e): given the adjoints of the hit point (gh) and of the normal
+// (gn), adds the adjoints of p and d and returns those of the element's radius and center.
+__device__ void intersect_adjoint(V3 p, V3 d, const SmemElement& e, V3 gh, V3 gn, V3& gp, V3& gd, float& gradius,
+                                  float& gcenter) {
+    if (e.radius == 0.0f) {  // plane z = -center: t = (-center - pz) / dz, hit = p + d t
+        const float t = (-e.center - p.z) / d.z;
+        const float gt = dot(gh, d);
+        gp = gp + gh;
+        gd = gd + gh * t;
+        gcenter += -gt / d.z;
+        gp.z += -gt / d.z;
+        gd.z += -gt * t / d.z;
+        return;
+    }
+    const float r = fabsf(e.radius), cz = -e.center;
+    const V3 u = v3(0.0f - p.x, 0.0f - p.y, cz - p.z);
+    const float proj = dot(u, d);
+    const V3 u1 = d * proj;
+    const V3 ev = u - u1;
+    const float dist2 = dot(ev, ev);
+    const float sgn = (e.radius * d.z) > 0.0f ? -1.0f : 1.0f;
+    const float m = sqrtf(fmaxf(r * r - dist2, 0.0f));
+    const V3 hit = (p + u1) - d * (m * sgn);
+    const V3 q = v3(hit.x, hit.y, hit.z - cz);
+    const float qn = sqrtf(dot(q, q));
+    // n = sgn q / |q|
+    const V3 qh = q * (1.0f / qn);
+    const V3 gq = (gn - qh * dot(qh, gn)) * (sgn / qn);
+    const V3 ghit = gh + gq;
+    float gcz = -gq.z;
+    // hit = p + u1 - sgn m d
+    gp = gp + ghit;
+    V3 gu1 = ghit;
+    const float gm = -sgn * dot(ghit, d);
+    gd = gd - ghit * (sgn * m);
+    // m = sqrt(r^2 - |e|^2) (a ray grazing the sphere, m = 0, gets no gradient through m)
+    V3 gu = v3(0.0f, 0.0f, 0.0f);
+    if (m > 1e-12f) {
+        const float gm2 = gm / (2.0f * m);
+        gradius += gm2 * 2.0f * e.radius;
+        const V3 ge = ev * (-2.0f * gm2);
+        // e = u - u1
+        gu = gu + ge;
+        gu1 = gu1 - ge;
+    }
+    // u1 = d proj
+    gd = gd + gu1 * proj;
+    const float gproj = dot(gu1, d);
+    // proj = u . d
+    gu = gu + d * gproj;
+    gd = gd + u * gproj;
+    // u = (0, 0, cz) - p
+    gcz += gu.z;
+    gp = gp - gu;
+    gcenter += -gcz;
+}
+
+__global__ void __launch_bounds__(kAdjThreads) k_trace_adjoint(const rf_lens_element* __restrict__ elements,
+                                                              const int2* __restrict__ paths,
+                                                              const float* __restrict__ wavelengths,
+                                                              const __grid_constant__ TraceParams p,
+                                                              const float* __restrict__ grad_rays,
+                                                              float* __restrict__ grad_elements,
+                                                              float* __restrict__ grad_dir) {
+    __shared__ SmemElement se[kAdjMaxElements];
+    __shared__ float ior_tab[kAdjTableRows * kAdjMaxElements];
+    __shared__ float acc[kAdjMaxElements * kGradPerElement + 3];
+    const int E = p.E;
+    const long long first = (long long)blockIdx.x * kAdjThreads;
+    const long long last = min(first + kAdjThreads, p.n_rays) - 1;
+    const long long pw_first = first / p.R, pw_last = last / p.R;
+    const long long span_rows = pw_last - pw_first + 1;
+    const int span = (int)(span_rows < (long long)p.W ? span_rows : (long long)p.W);
+    const bool table = span <= kAdjTableRows;
+    const bool disperse = !isnan(__ldg(&elements[0].coefficients[0]));
+    for (int i = threadIdx.x; i < E; i += kAdjThreads) {
+        const rf_lens_element& e = elements[i];
+        se[i].radius = e.radius;
+        se[i].center = e.center;
+        se[i].height = e.height;
+        se[i].ior = e.ior;
+        se[i].coating = e.coating;
+        se[i].layers = e.coating_layers;
+        se[i].d0 = e.coating_thickness[0];
+        se[i].d1 = e.coating_thickness[1];
+    }
+    if (table) {
+        for (int k = threadIdx.x; k < span * E; k += kAdjThreads) {
+            int row = k / E, el = k % E;
+            int wl = (int)((pw_first + row) % p.W);
+            float n = elements[el].ior;
+            if (disperse && n > 1.0f) n = dispersion(wavelengths[wl], elements[el].coefficients);
+            ior_tab[row * E + el] = n;
+        }
+    }
+    for (int i = threadIdx.x; i < E * kGradPerElement + 3; i += kAdjThreads) acc[i] = 0.0f;
+    __syncthreads();
+
+    float gE[kAdjMaxElements * kGradPerElement];
+#pragma unroll
+    for (int i = 0; i < kAdjMaxElements * kGradPerElement; i++) gE[i] = 0.0f;
+    V3 gdir = v3(0.0f, 0.0f, 0.0f);
+
+    const long long idx = first + threadIdx.x;
+    if (idx < p.n_rays) {
+        const long long n = p.n_rays;
+        const float g_out[6] = {grad_rays[idx], grad_rays[n + idx], grad_rays[2 * n + idx],
+                                grad_rays[3 * n + idx], grad_rays[4 * n + idx], grad_rays[5 * n + idx]};
+        const int ray_id = (int)(idx % p.R);
+        const long long pw = idx / p.R;
+        const int wl_id = (int)(pw % p.W);
+        const int path_id = (int)(pw / p.W);
+        const int row = (int)((pw - pw_first) % p.W);
+        const float* ior_row = table ? ior_tab + row * E : nullptr;
+        const float wavelength = __ldg(wavelengths + wl_id);
+        const float* coef_base = &elements[0].coefficients[0];
+        auto ior_of = [&](int el) -> float {
+            if (ior_row) return ior_row[el];
+            float nn = se[el].ior;
+            if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
+            return nn;
+        };
+        TraceFrame f;
+        f.E = E;
+        f.aperture = p.aperture;
+        f.W = p.W;
+        f.G = p.G;
+        f.R = p.R;
+        f.cmin = p.cmin;
+        f.layer_n0 = p.layer_n0;
+        f.layer_n1 = p.layer_n1;
+        f.dir[0] = p.dir[0];
+        f.dir[1] = p.dir[1];
+        f.dir[2] = p.dir[2];
+        const int gy = (int)truncf((float)ray_id / (float)p.G);
+        const int gx = ray_id - gy * p.G;
+        Step steps[kAdjMaxSteps];
+        StepRecorder rec{steps, 0, -1, 0.0f};
+        float out[6];
+        trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
+                      f, out, rec);
+        const bool valid = !isnan(out[5]) && rec.n <= kAdjMaxSteps && rec.n > 0;
+        if (valid) {
+            const float refl = out[5];
+            // adjoint of the state leaving the current step: position and direction
+            V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);
+            bool apt_pending = true;  // the last aperture crossing sets pos_apt
+            for (int j = rec.n - 1; j >= 0; j--) {
+                const Step& st = steps[j];
+                const int i = st.lens;
+                const SmemElement& e = se[i];
+                const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
+                const Hit h = intersect(pin.x, pin.y, pin.z, din.x, din.y, din.z, e);
+                V3 gh = gp;  // adjoint of the hit point
+                V3 gn = v3(0.0f, 0.0f, 0.0f);
+                V3 gdin = v3(0.0f, 0.0f, 0.0f);
+                if (j == rec.n - 1) gh = gh + v3(g_out[0], g_out[1], 0.0f);  // sensor position
+                if (i == p.aperture) {
+                    if (apt_pending) {
+                        gh.x += g_out[2] / e.height;
+                        gh.y += g_out[3] / e.height;
+                        apt_pending = false;
+                    }
+                    gdin = gd;  // no change of direction at the stop
+                } else {
+                    if (j == rec.argmax) {
+                        const float rxy = sqrtf(h.px * h.px + h.py * h.py);
+                        if (rxy > 0.0f) {
+                            const float s = g_out[4] / (rxy * e.height);
+                            gh.x += s * h.px;
+                            gh.y += s * h.py;
+                        }
+                    }
+                    const V3 nrm = v3(h.nx, h.ny, h.nz);
+                    if (i == E - 1) {
+                        gdin = gd;
+                    } else {
+                        const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
+                        const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
+                        const float n2 = ior_of(i);
+                        if (st.reflect) {
+                            // d' = d - 2 (d.n) n
+                            const float dn = dot(din, nrm), gdn = dot(gd, nrm);
+                            gdin = gd - nrm * (2.0f * gdn);
+                            gn = gn - (gd * dn + din * gdn) * 2.0f;
+                            // reflectance factor R(theta, thicknesses), refl *= R when R > 0
+                            const float c = -dn;
+                            const float cc = clampf(c, -1.0f, 1.0f);
+                            const float incident = acosf(cc);
+                            const float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
+                            D3 th = {theta, 1.0f, 0.0f, 0.0f};
+                            D3 R;
+                            float gtheta = 0.0f;
+                            if (e.layers == 2) {
+                                R = fresnel_two_layer_d(th, wavelength, n1, p.layer_n0, D3{e.d0, 0.f, 1.f, 0.f},
+                                                        p.layer_n1, D3{e.d1, 0.f, 0.f, 1.f}, n2);
+                            } else if (e.layers == 1 || e.coating > 0) {
+                                const float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
+                                const D3 d1 = e.layers == 1 ? D3{e.d0, 0.f, 1.f, 0.f}
+                                                            : dconst((float)e.coating / (4.0f * nc));
+                                R = fresnel_ar_d(th, wavelength, d1, n1, nc, n2);
+                            } else {
+                                R = fresnel_d(th, n1, n2);
+                            }
+                            if (R.v > 0.0f) {
+                                const float gR = g_out[5] * refl / R.v;
+                                gtheta = gR * R.g0;
+                                gE[i * kGradPerElement + 2] += gR * R.g1;
+                                gE[i * kGradPerElement + 3] += gR * R.g2;
+                            }
+                            if (fabsf(c) < 1.0f) {
+                                const float gc = gtheta * (-rsqrtf(1.0f - c * c));
+                                // c = -d.n
+                                gdin = gdin - nrm * gc;
+                                gn = gn - din * gc;
+                            }
+                        } else {
+                            // d' = o d + k n, k = o c - sqrt(1 - o^2 (1 - c^2)), c = -d.n
+                            const float o = n1 / n2;
+                            const float c = -dot(din, nrm);
+                            const float sint2 = (o * o) * (1.0f - c * c);
+                            const float sq = sqrtf(fabsf(1.0f - sint2));
+                            const float k = o * c - sq;
+                            const float gk = dot(gd, nrm);
+                            const float dk_dc = sq > 0.0f ? o - o * o * c / sq : o;
+                            gdin = gd * o - nrm * (gk * dk_dc);
+                            gn = gn + gd * k - din * (gk * dk_dc);
+                        }
+                    }
+                }
+                V3 gpin = v3(0.0f, 0.0f, 0.0f);
+                float gr = 0.0f, gc = 0.0f;
+                intersect_adjoint(pin, din, e, gh, gn, gpin, gdin, gr, gc);
+                gE[i * kGradPerElement + 0] += gr;
+                gE[i * kGradPerElement + 1] += gc;
+                gp = gpin;
+                gd = gdin;
+            }
+            // entry ray: p_in = hit0 - dir, d_in = dir; hit0 = grid point hitting element 0
+            gdir = gdir + gd - gp;
+            const V3 g0 = v3(p.grid[gx], -p.grid[gy], 1.0f);
+            const Hit h0 = intersect(g0.x, g0.y, g0.z, 0.0f, 0.0f, -1.0f, se[0]);
+            if (h0.hit) {
+                V3 gpg = v3(0.f, 0.f, 0.f), gdg = v3(0.f, 0.f, 0.f);
+                float gr = 0.0f, gc = 0.0f;
+                intersect_adjoint(g0, v3(0.0f, 0.0f, -1.0f), se[0], gp, v3(0.f, 0.f, 0.f), gpg, gdg, gr, gc);
+                gE[0] += gr;
+                gE[1] += gc;
+            }
+        }
+    }
+    // warp sums, then one shared-memory add per warp and value, then global
+    const int lane = threadIdx.x & 31;
+    for (int i = 0; i < E * kGradPerElement; i++) {
+        float v = gE[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(&acc[i], v);
+    }
+    float dv[3] = {gdir.x, gdir.y, gdir.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float v = dv[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(&acc[E * kGradPerElement + k], v);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < E * kGradPerElement; i += kAdjThreads)
+        if (acc[i] != 0.0f) atomicAdd(&grad_elements[i], acc[i]);
+    if (threadIdx.x < 3 && acc[E * kGradPerElement + threadIdx.x] != 0.0f)
+        atomicAdd(&grad_dir[threadIdx.x], acc[E * kGradPerElement + threadIdx.x]);
+}
+
+}  // namespace
+}  // namespace rf
+
+extern "C" int rf_trace_adjoint(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
+                                const rf_trace_args* args, const float* grad_rays, float* grad_elements,
+                                float* grad_direction, void* stream) {
+    using namespace rf;
+    if (!elements || !paths || !wavelengths || !args || !grad_rays || !grad_elements || !grad_direction)
+        return RF_ERR_INVALID_ARG;
+    const rf_trace_args& a = *args;
+    if (a.element_count < 2 || a.element_count > kAdjMaxElements || a.path_count < 0 || a.wavelength_count < 1 ||
+        a.grid_count < 2 || a.grid_count > kMaxGrid || a.aperture_index < 0)
+        return RF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    RF_TRY(cuda_status(
+        cudaMemsetAsync(grad_elements, 0, sizeof(float) * kGradPerElement * (size_t)a.element_count, s)));
+    RF_TRY(cuda_status(cudaMemsetAsync(grad_direction, 0, sizeof(float) * 3, s)));
+    TraceParams p;
+    if (!trace_params(a, p)) return RF_ERR_INVALID_ARG;
+    if (p.n_rays == 0) return RF_OK;
+    k_trace_adjoint<<<blocks_for(p.n_rays, kAdjThreads), kAdjThreads, 0, s>>>(elements, (const int2*)paths,
+                                                                           wavelengths, p, grad_rays, grad_elements,
+                                                                           grad_direction);
+    return launch_status();
+}

@@ -150,6 +150,122 @@ __global__ void __launch_bounds__(kThreads) k_vertex(const float* __restrict__ r
                (long long)blockIdx.x * kThreads + threadIdx.x);
 }
 
+// ---------------------------------------------------------------- adjoints
+// Vertex i (ray-plane order): the aperture position, rrel and reflectance gradients pass to
+// the ray unchanged; the intensity gradient goes to the neighbour quads whose positive
+// intensities the vertex averaged (vertex_shader, rasterizing.cl:362-369).
+__global__ void __launch_bounds__(kThreads) k_vertex_backward(const float* __restrict__ rays,
+                                                              const float* __restrict__ inten, int W, int G,
+                                                              long long n_rays, const float* __restrict__ grad_vtx,
+                                                              float* __restrict__ grad_rays,
+                                                              float* __restrict__ grad_inten) {
+    const int Q = (G - 1) * (G - 1), R = G * G;
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n_rays) return;
+    const int ray_id = (int)(i % R);
+    const long long pw = i / R;
+    const int w = (int)(pw % W);
+    const long long path = pw / W;
+    const long long vi = (path * R + ray_id) * W + w;
+    const float refl = __ldg(rays + 5 * n_rays + i);
+    const float* g = grad_vtx + 8 * vi;
+    const bool valid = !isnan(refl);
+    grad_rays[2 * n_rays + i] = valid ? g[2] : 0.0f;
+    grad_rays[3 * n_rays + i] = valid ? g[3] : 0.0f;
+    grad_rays[4 * n_rays + i] = valid ? g[4] : 0.0f;
+    grad_rays[5 * n_rays + i] = valid ? g[5] : 0.0f;
+    const float gi = g[6];
+    if (!valid || gi == 0.0f) return;
+    const int x = ray_id % G, y = ray_id / G;
+    int nb[4];
+    nb[0] = (y - 1) * (G - 1) + (x - 1);
+    nb[1] = nb[0] + 1;
+    nb[2] = y * (G - 1) + (x - 1);
+    nb[3] = nb[2] + 1;
+    int count = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (nb[k] >= 0 && nb[k] < Q && __ldg(inten + ((size_t)path * Q + nb[k]) * W + w) > 0.0f) ++count;
+    const float share = gi / (float)(count > 1 ? count : 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (nb[k] < 0 || nb[k] >= Q) continue;
+        const size_t qi = ((size_t)path * Q + nb[k]) * W + w;
+        if (__ldg(inten + qi) > 0.0f) atomicAdd(grad_inten + qi, share);
+    }
+}
+
+// d edge_f(a, b, c) / d(ax, ay, bx, by, cx, cy), scaled by s and added to g[2 * slot]
+__device__ __forceinline__ void edge_grad(const float* x, const float* y, int a, int b, int c, float s, float* gx,
+                                          float* gy) {
+    gx[a] += s * (y[c] - y[b]);
+    gy[a] += s * (x[b] - x[c]);
+    gx[b] += s * (y[a] - y[c]);
+    gy[b] += s * (x[c] - x[a]);
+    gx[c] += s * (y[b] - y[a]);
+    gy[c] += s * (x[a] - x[b]);
+}
+
+// Primitive pq: intensity = area_orig / max(area, min_area) (prim_shader,
+// rasterizing.cl:271-301) passes its gradient to the sensor positions of the corner rays.
+__global__ void __launch_bounds__(kThreads) k_quad_setup_backward(const float* __restrict__ rays, int P, int W, int G,
+                                                                  long long n_rays, float area_orig, float min_area,
+                                                                  const float* __restrict__ grad_inten,
+                                                                  float* __restrict__ grad_rays) {
+    const int Q = (G - 1) * (G - 1), R = G * G;
+    const long long pq = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (pq >= (long long)P * Q) return;
+    const int path = (int)(pq / Q), quad = (int)(pq % Q);
+    const int row = quad / (G - 1), col = quad % (G - 1);
+    int v[4];
+    v[0] = row * G + col;
+    v[1] = v[0] + 1;
+    v[2] = v[1] + G;
+    v[3] = v[0] + G;
+    for (int w = 0; w < W; w++) {
+        const size_t off = ((size_t)path * W + w) * R;
+        float px[4], py[4];
+        int src[4];
+        int valid = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            if (!isnan(__ldg(rays + 5 * n_rays + off + v[i]))) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (k == valid) {
+                        px[k] = __ldg(rays + off + v[i]);
+                        py[k] = __ldg(rays + n_rays + off + v[i]);
+                        src[k] = v[i];
+                    }
+                valid++;
+            }
+        }
+        if (valid < 3) break;  // the forward culls this and every later wavelength
+        const float g = __ldg(grad_inten + (size_t)pq * W + w);
+        if (g == 0.0f) continue;
+        float area, sa;
+        float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+        if (valid == 4) {
+            const float a0 = edge_f(px[0], py[0], px[1], py[1], px[2], py[2]);
+            const float a1 = edge_f(px[0], py[0], px[2], py[2], px[3], py[3]);
+            area = fabsf(a0 + a1) / 2.0f;
+            sa = (a0 + a1 >= 0.0f ? 0.5f : -0.5f);
+        } else {
+            const float a0 = edge_f(px[0], py[0], px[1], py[1], px[2], py[2]);
+            area = fabsf(a0);
+            sa = a0 >= 0.0f ? 1.0f : -1.0f;
+        }
+        if (!(area > min_area)) continue;  // max(area, min_area) holds min_area: no gradient
+        const float g_area = -area_orig / (area * area) * g;
+        edge_grad(px, py, 0, 1, 2, g_area * sa, gx, gy);
+        if (valid == 4) edge_grad(px, py, 0, 2, 3, g_area * sa, gx, gy);
+        for (int k = 0; k < valid; k++) {
+            atomicAdd(grad_rays + off + src[k], gx[k]);
+            atomicAdd(grad_rays + n_rays + off + src[k], gy[k]);
+        }
+    }
+}
+
 // Batched forms: block b works for the frame whose first block of the stage is the largest
 // one <= b.
 __global__ void __launch_bounds__(kThreads) k_quad_setup_batch(const rf_frame* __restrict__ frames, int F,
@@ -241,5 +357,37 @@ extern "C" int rf_vertex_batch(const rf_frame* frames, const rf_batch_sizes* siz
     if (sizes->vertex_blocks > 0x7fffffffLL) return RF_ERR_NOT_SUPPORTED;
     k_vertex_batch<<<(unsigned)sizes->vertex_blocks, kThreads, 0, (cudaStream_t)stream>>>(
         frames, sizes->frame_count, rays, intensities, (float4*)vertexes);
+    return launch_status();
+}
+
+extern "C" int rf_vertex_backward(const float* rays, const float* intensities, int32_t path_count,
+                                  int32_t wavelength_count, int32_t grid_count, const float* grad_vertexes,
+                                  float* grad_rays, float* grad_intensities, void* stream) {
+    using namespace rf;
+    if (!rays || !intensities || !grad_vertexes || !grad_rays || !grad_intensities || path_count < 0 ||
+        wavelength_count < 1 || grid_count < 2)
+        return RF_ERR_INVALID_ARG;
+    const long long n_rays = (long long)path_count * wavelength_count * grid_count * grid_count;
+    const long long n_inten = (long long)path_count * (grid_count - 1) * (grid_count - 1) * wavelength_count;
+    cudaStream_t s = (cudaStream_t)stream;
+    RF_TRY(cuda_status(cudaMemsetAsync(grad_intensities, 0, sizeof(float) * (size_t)n_inten, s)));
+    RF_TRY(cuda_status(cudaMemsetAsync(grad_rays, 0, sizeof(float) * 2 * (size_t)n_rays, s)));
+    if (n_rays == 0) return RF_OK;
+    k_vertex_backward<<<blocks_for(n_rays, kThreads), kThreads, 0, s>>>(
+        rays, intensities, wavelength_count, grid_count, n_rays, grad_vertexes, grad_rays, grad_intensities);
+    return launch_status();
+}
+
+extern "C" int rf_quad_setup_backward(const float* rays, int32_t path_count, int32_t wavelength_count,
+                                      int32_t grid_count, float area_orig, float min_area,
+                                      const float* grad_intensities, float* grad_rays, void* stream) {
+    using namespace rf;
+    if (!rays || !grad_intensities || !grad_rays || path_count < 0 || wavelength_count < 1 || grid_count < 2)
+        return RF_ERR_INVALID_ARG;
+    const long long n = (long long)path_count * (grid_count - 1) * (grid_count - 1);
+    if (n == 0) return RF_OK;
+    const long long n_rays = (long long)path_count * wavelength_count * grid_count * grid_count;
+    k_quad_setup_backward<<<blocks_for(n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        rays, path_count, wavelength_count, grid_count, n_rays, area_orig, min_area, grad_intensities, grad_rays);
     return launch_status();
 }

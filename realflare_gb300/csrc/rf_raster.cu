@@ -572,6 +572,249 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
     }
 }
 
+// ---------------------------------------------------------------- adjoint
+// ghost_sample with its derivatives with respect to the texel coordinates (u, v).
+__device__ __forceinline__ float ghost_sample_grad(const float* __restrict__ tex, int w, int h, float u, float v,
+                                                   float& du, float& dv) {
+    du = dv = 0.0f;
+    if (!(fabsf(u) < 1e9f) || !(fabsf(v) < 1e9f)) return 0.0f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const int i0 = (int)fu, j0 = (int)fv;
+    const bool i0_in = (unsigned)i0 < (unsigned)w, i1_in = (unsigned)(i0 + 1) < (unsigned)w;
+    const bool j0_in = (unsigned)j0 < (unsigned)h, j1_in = (unsigned)(j0 + 1) < (unsigned)h;
+    const int ia = min(max(i0, 0), w - 1), ib = min(max(i0 + 1, 0), w - 1);
+    const float* row0 = tex + (size_t)min(max(j0, 0), h - 1) * w;
+    const float* row1 = tex + (size_t)min(max(j0 + 1, 0), h - 1) * w;
+    const float t00 = (i0_in && j0_in) ? __ldg(row0 + ia) : 0.0f;
+    const float t10 = (i1_in && j0_in) ? __ldg(row0 + ib) : 0.0f;
+    const float t01 = (i0_in && j1_in) ? __ldg(row1 + ia) : 0.0f;
+    const float t11 = (i1_in && j1_in) ? __ldg(row1 + ib) : 0.0f;
+    du = (1.0f - b) * (t10 - t00) + b * (t11 - t01);
+    dv = (1.0f - a) * (t01 - t00) + a * (t11 - t10);
+    return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
+}
+
+constexpr int kGradAttrs = 5;  // per corner: u, v, rrel, reflectance, intensity
+// vertex float of each attribute (pos.xy, uv.xy, rrel, reflectance, intensity, pad)
+__device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6};
+
+// Backward of k_raster for 32 x 32 tiles: the same tiles, entry lists, records, coverage
+// and mean-value weights as the forward (held fixed: they are piecewise constant in the
+// vertex positions), differentiating each fragment with respect to the attributes its
+// corners interpolate. Per record the warp sums its pixels' contributions with shuffles;
+// the CTA sums warps in shared memory and adds each record's totals to the two vertices
+// (wavelength pair endpoints) of each corner once per tile.
+__global__ void __launch_bounds__(kThreads, 2)
+    k_raster_backward(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
+                      const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
+                      const float* __restrict__ spectrum, RasterParams p, FragmentConsts fc,
+                      const float4* __restrict__ image, const float4* __restrict__ grad_image,
+                      float* __restrict__ grad_vtx) {
+    constexpr int T = 32, kBlocks = 32, kCols = 4;
+    extern __shared__ float4 smem4[];
+    Rec* recs = (Rec*)smem4;
+    float* xyz = (float*)(recs + kBatchRecords);
+    float* blend = xyz + 3 * p.maxW * p.WS;
+    float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
+    float* rgrad = grgb + 96 * kBlocks;                // [record][corner * 5 + attribute]
+    const int tile = blockIdx.x;
+    const int tx = tile % p.ntx, ty = tile / p.ntx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        const float sub_step = 1.0f / (float)p.WS;
+        float b = 0.0f;
+        for (int i = 0; i < p.WS; i++) {
+            blend[i] = b;
+            b += sub_step;
+        }
+    }
+    if (p.W > 1) {
+        const float sub_step = 1.0f / (float)p.WS;
+        const float wl_step = sub_step / (float)p.W;
+        for (int w = threadIdx.x; w < p.maxW; w += kThreads) {
+            float pos = ((float)w + 0.5f) / (float)p.W;
+            for (int i = 0; i < p.WS; i++) {
+                for (int c = 0; c < 3; c++)
+                    xyz[3 * (w * p.WS + i) + c] = sample_linear(spectrum, RF_SPECTRUM_WIDTH, 1, 4, c, pos, 0.0f, true);
+                pos += wl_step;
+            }
+        }
+    }
+    // out = AP1(rgb * scale) where any channel of rgb is positive, else 0
+    const float scale = p.intensity / (float)(p.W * p.S * p.WS);
+    const float4 m0 = xyz_to_ap1(1.0f, 0.0f, 0.0f), m1 = xyz_to_ap1(0.0f, 1.0f, 0.0f),
+                 m2 = xyz_to_ap1(0.0f, 0.0f, 1.0f);
+#pragma unroll
+    for (int k = 0; k < kBlocks / 8; k++) {
+        const int blk = warp + 8 * k;
+        const int px = tx * T + (blk % kCols) * 8 + (lane & 7), py = ty * T + (blk / kCols) * 4 + (lane >> 3);
+        float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+        if (px < p.width && py < p.height) {
+            const size_t o = (size_t)(p.height - (py + 1)) * p.width + px;
+            const float4 out = image[o], g = grad_image[o];
+            if (out.x != 0.0f || out.y != 0.0f || out.z != 0.0f) {
+                g0 = scale * (m0.x * g.x + m0.y * g.y + m0.z * g.z);
+                g1 = scale * (m1.x * g.x + m1.y * g.y + m1.z * g.z);
+                g2 = scale * (m2.x * g.x + m2.y * g.y + m2.z * g.z);
+            }
+        }
+        grgb[(3 * blk) * 32 + lane] = g0;
+        grgb[(3 * blk + 1) * 32 + lane] = g1;
+        grgb[(3 * blk + 2) * 32 + lane] = g2;
+    }
+    for (int i = threadIdx.x; i < kBatchRecords * 4 * kGradAttrs; i += kThreads) rgrad[i] = 0.0f;
+
+    const int S = p.S;
+    const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
+    const int per_batch = kBatchRecords / p.WS;
+    const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
+    const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
+    for (uint32_t base = begin; base < end; base += per_batch) {
+        const int n_rec = (int)min((uint32_t)per_batch, end - base) * p.WS;
+        __syncthreads();  // blend, colours and pixel gradients set; the previous batch flushed
+        for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
+            const int e = my_entry + 64 * h;
+            if (e < per_batch && base + e < end) {
+                CornerLoad c;
+                load_corner(vtx, tile_entries[base + e], my_corner, p, c);
+                for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, recs[e * p.WS + i]);
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n_rec; j += kThreads) {
+            const uint32_t entry = tile_entries[base + j / p.WS];
+            finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int k = 0; k < kBlocks / 8; k++) {
+            const int blk = warp + 8 * k;
+            const int x0 = tx * T + (blk % kCols) * 8, y0 = ty * T + (blk / kCols) * 4;
+            const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
+            const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
+            const bool in_image = px < p.width && py < p.height;
+            const int sx0 = px * S, sy0 = py * S;
+            const float g0 = grgb[(3 * blk) * 32 + lane], g1 = grgb[(3 * blk + 1) * 32 + lane],
+                        g2 = grgb[(3 * blk + 2) * 32 + lane];
+            const bool any_grad = __any_sync(0xffffffffu, g0 != 0.0f || g1 != 0.0f || g2 != 0.0f);
+            if (!any_grad) continue;
+            unsigned sel[kBatchRecords / 32], whole[kBatchRecords / 32];
+#pragma unroll
+            for (int m = 0; m < kBatchRecords / 32; m++) {
+                const int j = m * 32 + lane;
+                bool take = false, all = false;
+                if (j < n_rec) {
+                    const Rec& r = recs[j];
+                    const int flags = r.flags;
+                    if (!(flags & 2)) {
+                        const int4 bb = *reinterpret_cast<const int4*>(r.bb);
+                        take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);
+                        if (take && (flags & 1)) {
+                            const int cov = rect_coverage(r, bx0, bx1, by0, by1);
+                            take = cov != 0;
+                            all = cov == 2;
+                        }
+                    }
+                }
+                sel[m] = __ballot_sync(0xffffffffu, take);
+                whole[m] = __ballot_sync(0xffffffffu, all);
+            }
+#pragma unroll
+            for (int m = 0; m < kBatchRecords / 32; m++) {
+                unsigned bits = sel[m];
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    const int j = m * 32 + b;
+                    bits &= bits - 1;
+                    const Rec& r = recs[j];
+                    int hits = 0;
+                    if (in_image) {
+                        if ((whole[m] >> b) & 1u) {
+                            hits = S;
+                        } else {
+                            bool test = true;
+                            if (r.flags & 1) {
+                                const int4 bb = *reinterpret_cast<const int4*>(r.bb);
+                                test = !(sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w);
+                            }
+                            if (test)
+                                for (int s = 0; s < S; s++)
+                                    hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
+                        }
+                    }
+                    float gw[kGradAttrs] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                    float wt[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (hits > 0) {
+                        barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
+                        float dLdf;
+                        if (p.W > 1) {
+                            const float* c = xyz + 3 * r.color;
+                            dLdf = g0 * c[0] + g1 * c[1] + g2 * c[2];
+                        } else {
+                            dLdf = g0 + g1 + g2;
+                        }
+                        const float u = wt[0] * r.uv[0] + wt[1] * r.uv[2] + wt[2] * r.uv[4] + wt[3] * r.uv[6];
+                        const float v = wt[0] * r.uv[1] + wt[1] * r.uv[3] + wt[2] * r.uv[5] + wt[3] * r.uv[7];
+                        float dgu, dgv;
+                        const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox,
+                                                           v * fc.tsy + fc.toy, dgu, dgv);
+                        const float rr = wt[0] * r.rrel[0] + wt[1] * r.rrel[1] + wt[2] * r.rrel[2] + wt[3] * r.rrel[3];
+                        const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
+                        const float ri = st * st * (3.0f - 2.0f * st);
+                        const float dri = (st > 0.0f && st < 1.0f) ? 6.0f * st * (1.0f - st) * (1.0f / (0.95f - 1.0f))
+                                                                  : 0.0f;
+                        const float ai_raw = wt[0] * r.inten[0] + wt[1] * r.inten[1] + wt[2] * r.inten[2] +
+                                             wt[3] * r.inten[3];
+                        const float ci_raw = wt[0] * r.refl[0] + wt[1] * r.refl[1] + wt[2] * r.refl[2] +
+                                             wt[3] * r.refl[3];
+                        const float ai = fmaxf(ai_raw, 0.0f), ci = fmaxf(ci_raw, 0.0f);
+                        const float H = (float)hits;
+                        const float d = dLdf * H;
+                        gw[0] = d * ri * ai * ci * dgu * fc.tsx;
+                        gw[1] = d * ri * ai * ci * dgv * fc.tsy;
+                        gw[2] = d * gi * ai * ci * dri;
+                        gw[3] = ci_raw > 0.0f ? d * gi * ri * ai : 0.0f;
+                        gw[4] = ai_raw > 0.0f ? d * gi * ri * ci : 0.0f;
+                    }
+                    // the warp's sum of each corner attribute's gradient
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+#pragma unroll
+                        for (int a = 0; a < kGradAttrs; a++) {
+                            float val = gw[a] * wt[c];
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                            if (lane == c * kGradAttrs + a && val != 0.0f)
+                                atomicAdd(&rgrad[j * 4 * kGradAttrs + c * kGradAttrs + a], val);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // each record's gradients to the two vertices of each corner (mix_vertex weights)
+        for (int idx = threadIdx.x; idx < n_rec * 4 * kGradAttrs; idx += kThreads) {
+            const float g = rgrad[idx];
+            if (g == 0.0f) continue;
+            rgrad[idx] = 0.0f;
+            const int j = idx / (4 * kGradAttrs), rem = idx % (4 * kGradAttrs);
+            const int corner = rem / kGradAttrs, a = rem % kGradAttrs;
+            const uint32_t entry = tile_entries[base + j / p.WS];
+            const float t = blend[j % p.WS];
+            const long long prim = entry / p.maxW;
+            const int w = (int)(entry % p.maxW);
+            const long long path = prim / Q;
+            const int quad = (int)(prim % Q);
+            const int c0 = (quad / (p.G - 1)) * p.G + quad % (p.G - 1);
+            const int cv = corner == 0 ? c0 : (corner == 1 ? c0 + 1 : (corner == 2 ? c0 + 1 + p.G : c0 + p.G));
+            const long long vi = (path * VC + cv) * p.W + w;
+            atomicAdd(grad_vtx + 8 * vi + kGradSlot[a], g * (1.0f - t));
+            atomicAdd(grad_vtx + 8 * (vi + 1) + kGradSlot[a], g * t);
+        }
+    }
+}
+
 // The reference's own loop: every pixel scans every mask of its bin (rasterizing.cl:573-654).
 __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__ vtx,
                                                       const unsigned long long* __restrict__ masks, int batch_count,
@@ -798,6 +1041,34 @@ extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int
     k_raster_masks<<<grid, 256, 0, (cudaStream_t)stream>>>((const float4*)vertexes, (const unsigned long long*)masks,
                                                            batch_count, args->bin_size, prim_total, ghost, spectrum,
                                                            p, fragment_consts(p), (float4*)image);
+    return launch_status();
+}
+
+extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                                  const float* ghost, const float* spectrum, const rf_raster_args* args,
+                                  const float* image, const float* grad_image, float* grad_vertexes, void* stream) {
+    using namespace rf;
+    if (!vertexes || !tile_offsets || !ghost || !spectrum || !args || !image || !grad_image || !grad_vertexes)
+        return RF_ERR_INVALID_ARG;
+    if (!aligned16(vertexes) || !aligned16(image) || !aligned16(grad_image)) return RF_ERR_INVALID_ARG;
+    RasterParams p;
+    if (!make_params(*args, p)) return RF_ERR_INVALID_ARG;
+    if (p.WS > kBatchRecords || p.maxW * p.WS > 4096) return RF_ERR_INVALID_ARG;
+    if (tile_size_of(*args) != 32) return RF_ERR_NOT_SUPPORTED;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n_vertices = (long long)args->path_count * args->grid_count * args->grid_count *
+                                 args->wavelength_count + 1;
+    RF_TRY(cuda_status(cudaMemsetAsync(grad_vertexes, 0, sizeof(float) * 8 * (size_t)n_vertices, s)));
+    p.T = 32;
+    p.ntx = (p.width + 31) / 32;
+    const int nty = (p.height + 31) / 32;
+    const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
+                        sizeof(float) * (96 * 32 + kBatchRecords * 4 * kGradAttrs);
+    static std::atomic<size_t> allowed[kMaxDevices];
+    RF_TRY(allow_smem(k_raster_backward, smem, allowed));
+    k_raster_backward<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries, ghost,
+                                                         spectrum, p, fragment_consts(p), (const float4*)image,
+                                                         (const float4*)grad_image, grad_vertexes);
     return launch_status();
 }
 

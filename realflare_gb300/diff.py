@@ -1,0 +1,240 @@
+"""Differentiable flare rendering: the gradient of an image loss with respect to the lens
+surfaces' curvature radii, the axial gaps between them, their coating thicknesses and the
+light position. No reference counterpart (the reference renders only).
+
+``LensParameters`` maps the free parameters to the trace's per-element inputs with torch
+operations (so torch differentiates the mapping): element ``center = sum of the previous
+elements' distances + radius``, the stop halving the gap it sits in, and the light direction
+``(x * sensor_w / 2, y * h / w * sensor_w / 2, focal_length)``. ``FlareFunction`` (a
+``torch.autograd.Function``) renders the flare with the CUDA kernels and, in backward, runs
+their adjoints: ``rf_raster_backward`` (a gather over the forward's tile lists),
+``rf_vertex_backward``, ``rf_quad_setup_backward`` (the 1/quad-area intensity term) and
+``rf_trace_adjoint`` (rays re-traced from their entry point, surfaces recomputed).
+
+What the gradient includes: ray positions through the quad-area intensity and through the
+aperture positions (ghost texture lookup) and rrel, the Fresnel/coating reflectance, and the
+light direction through all of these. What it leaves out, by construction: coverage. Which
+pixels a quad covers and its mean-value weights depend on the vertex positions only through
+integer sample coordinates (the reference truncates them), so they are piecewise constant;
+the change of covered pixels as quad edges move, including a ghost sliding across the
+screen, is not part of the gradient. The gradient is the derivative of the rendered image
+wherever no coverage changes.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import prepare
+from ._abi import check, lib
+from .data import Project, RealflareError
+from .device import empty, require_cuda
+
+
+@dataclass
+class LensLayout:
+    """Element-level structure of a lens model: which elements are free surfaces, where the
+    stop sits, and the constants of the mapping."""
+    surfaces: list          # element indices of the spherical surfaces (the stop excluded)
+    stop: int               # element index of the stop
+    back_distance: float    # distance of the last surface to the sensor (held fixed)
+    base_distances: np.ndarray  # element distances of the model
+    focal_length: float
+    sensor_w: float
+    aspect: float           # image height / width
+
+
+def layout(project: Project) -> LensLayout:
+    lens = project.flare.lens
+    model = lens.lens_model
+    if model is None:
+        raise RealflareError('differentiation needs a lens model object')
+    n = len(model.lens_elements)
+    surfaces = [i for i in range(n) if i != model.aperture_index]
+    dist = np.array([e.distance for e in model.lens_elements], np.float64)
+    r = project.render.resolution
+    return LensLayout(surfaces, model.aperture_index, float(dist[-1]), dist, float(model.focal_length),
+                      float(lens.sensor_size.width()), r.height() / r.width())
+
+
+class LensParameters:
+    """The free parameters of a lens and light: ``radii`` (one per surface), ``gaps`` (axial
+    distance from each surface to the next; a stop inside a gap sits at its middle),
+    ``thickness`` (single-layer coating thickness in nm per surface) and ``light`` (the
+    normalised field position)."""
+
+    def __init__(self, project: Project, device=None) -> None:
+        self.project = project
+        self.layout = layout(project)
+        lo = self.layout
+        model = project.flare.lens.lens_model
+        dev = device if device is not None else require_cuda()
+        el = model.lens_elements
+        radii = [el[i].radius for i in lo.surfaces]
+        gaps = []
+        for k in range(len(lo.surfaces) - 1):
+            a, b = lo.surfaces[k], lo.surfaces[k + 1]
+            gaps.append(float(sum(lo.base_distances[a:b])))
+        thick = project.flare.lens.coating_thickness
+        t = [float(thick[i]) if i < len(thick) and np.ndim(thick[i]) == 0 else 0.0 for i in lo.surfaces]
+        pos = project.flare.light.position
+        kw = dict(dtype=torch.float64, device=dev)
+        self.radii = torch.tensor(radii, **kw)
+        self.gaps = torch.tensor(gaps, **kw)
+        self.thickness = torch.tensor(t, **kw)
+        self.light = torch.tensor([pos.x(), pos.y()], **kw)
+
+    def tensors(self) -> list:
+        return [self.radii, self.gaps, self.thickness, self.light]
+
+    def elements(self, radii, gaps, thickness, light, n_elements: int):
+        """(radius, center, thickness, direction.xyz) per element as torch tensors."""
+        lo = self.layout
+        dev, dt = radii.device, radii.dtype
+        radius = torch.zeros(n_elements, device=dev, dtype=dt)
+        radius = radius.index_put((torch.tensor(lo.surfaces, device=dev),), radii)
+        # element distances: surface k's distance is its gap (half of it before the stop,
+        # the stop taking the other half); the last surface keeps its back distance
+        distances = []
+        for k, s in enumerate(lo.surfaces):
+            if k == len(lo.surfaces) - 1:
+                distances.append(torch.tensor(lo.back_distance, device=dev, dtype=dt))
+            elif lo.surfaces[k + 1] == s + 1:
+                distances.append(gaps[k])
+            else:  # the stop sits between s and the next surface
+                distances.append(gaps[k] / 2)
+                distances.append(gaps[k] / 2)
+        distances.append(torch.tensor(0.0, device=dev, dtype=dt))  # the sensor
+        d = torch.stack(distances)
+        offset = torch.cat([torch.zeros(1, device=dev, dtype=dt), torch.cumsum(d, 0)[:-1]])
+        center = offset + radius
+        t = torch.zeros(n_elements, device=dev, dtype=dt)
+        t = t.index_put((torch.tensor(lo.surfaces, device=dev),), thickness)
+        direction = torch.stack([light[0] * lo.sensor_w / 2, light[1] * lo.aspect * lo.sensor_w / 2,
+                                 torch.tensor(lo.focal_length, device=dev, dtype=dt)])
+        return radius, center, t, direction
+
+
+class DifferentiableRenderer:
+    """The flare of one project (lens, ghosts, wavelengths, grid, image) as a differentiable
+    function of ``LensParameters``. ``render(params)`` returns the (h, w, 4) image tensor."""
+
+    def __init__(self, project: Project, ghost: torch.Tensor, paths=None, stream=None) -> None:
+        from .tasks import RasterizingTask
+
+        require_cuda()
+        self.lib = lib()
+        self.project = project
+        self.ghost = ghost
+        self.inputs = prepare.trace_inputs(project, paths)
+        if self.inputs is None:
+            raise RealflareError('the lens has fewer than two elements')
+        ti = self.inputs
+        self.E = ti.args.element_count
+        if np.any(ti.elements['coating_layers'][[i for i in range(self.E - 1)]] == 2):
+            raise RealflareError('differentiation supports single-layer coatings')
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        dev = require_cuda()
+        self.base_elements = torch.from_numpy(ti.elements.view(np.float32).reshape(self.E, 16).copy()).to(dev)
+        self.paths = torch.from_numpy(ti.paths).to(dev)
+        self.wavelengths = torch.from_numpy(ti.wavelengths).to(dev)
+        a = ti.args
+        self.P, self.W, self.G = a.path_count, a.wavelength_count, a.grid_count
+        self.n_rays = ti.ray_count
+        self.area, self.min_area = prepare.quad_constants(project)
+        self.raster_args = prepare.raster_args(project, self.P, self.W, tuple(ghost.shape[:2]), tile_size=32)
+        self.task = RasterizingTask(self.stream)
+        self.rays = empty((6, max(self.n_rays, 1)))
+        self.params = LensParameters(project, dev)
+
+    # -- kernels --------------------------------------------------------------------
+    def _element_buffer(self, radius, center, thickness) -> torch.Tensor:
+        el = self.base_elements.clone()
+        el[:, 0] = radius.to(torch.float32)
+        el[:, 3] = center.to(torch.float32)
+        el[:, 6] = thickness.to(torch.float32)
+        return el
+
+    def _trace_args(self, direction):
+        a = prepare.TraceArgs.from_buffer_copy(self.inputs.args)
+        d = direction.detach().to(torch.float32).cpu().tolist()
+        for k in range(3):
+            a.direction[k] = d[k]
+        return a
+
+    def forward_kernels(self, radius, center, thickness, direction) -> torch.Tensor:
+        s = int(self.stream.cuda_stream)
+        self.el = self._element_buffer(radius, center, thickness)
+        self.targs = self._trace_args(direction)
+        check(self.lib.rf_trace(self.el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(),
+                                ctypes.byref(self.targs), self.rays.data_ptr(), s), 'rf_trace')
+        from .device import Rays
+
+        rays = Rays(self.rays, (self.P, self.W, self.G ** 2))
+        self.bounds, self.inten, self.vtx = self.task.setup(self.project, rays)
+        self.offsets, self.entries = self.task.bin(self.raster_args, self.bounds, self.vtx)
+        h, w = self.raster_args.height, self.raster_args.width
+        self.image = empty((h, w, 4))
+        check(self.lib.rf_raster(self.vtx.data_ptr(), self.offsets.data_ptr(), self.entries.data_ptr(),
+                                 self.ghost.data_ptr(), self.task.spectrum().data_ptr(), ctypes.byref(self.raster_args),
+                                 self.image.data_ptr(), s), 'rf_raster')
+        return self.image
+
+    def backward_kernels(self, grad_image: torch.Tensor):
+        """(grad radius, grad center, grad thickness per element, grad normalised direction)."""
+        s = int(self.stream.cuda_stream)
+        gi = grad_image.to(torch.float32).contiguous()
+        n_vtx = self.P * self.G ** 2 * self.W + 1
+        g_vtx = empty((n_vtx * 8,))
+        check(self.lib.rf_raster_backward(self.vtx.data_ptr(), self.offsets.data_ptr(), self.entries.data_ptr(),
+                                          self.ghost.data_ptr(), self.task.spectrum().data_ptr(),
+                                          ctypes.byref(self.raster_args), self.image.data_ptr(), gi.data_ptr(),
+                                          g_vtx.data_ptr(), s), 'rf_raster_backward')
+        g_rays = empty((6, max(self.n_rays, 1)))
+        g_inten = empty((max(self.P * (self.G - 1) ** 2 * self.W, 1),))
+        check(self.lib.rf_vertex_backward(self.rays.data_ptr(), self.inten.data_ptr(), self.P, self.W, self.G,
+                                          g_vtx.data_ptr(), g_rays.data_ptr(), g_inten.data_ptr(), s),
+              'rf_vertex_backward')
+        check(self.lib.rf_quad_setup_backward(self.rays.data_ptr(), self.P, self.W, self.G, self.area, self.min_area,
+                                              g_inten.data_ptr(), g_rays.data_ptr(), s), 'rf_quad_setup_backward')
+        g_el = empty((self.E, 4))
+        g_dir = empty((3,))
+        check(self.lib.rf_trace_adjoint(self.el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(),
+                                        ctypes.byref(self.targs), g_rays.data_ptr(), g_el.data_ptr(), g_dir.data_ptr(),
+                                        s), 'rf_trace_adjoint')
+        self.grad_rays = g_rays
+        return g_el[:, 0], g_el[:, 1], g_el[:, 2], g_dir
+
+    # -- torch ----------------------------------------------------------------------
+    def render(self, radii, gaps, thickness, light) -> torch.Tensor:
+        radius, center, t, direction = self.params.elements(radii, gaps, thickness, light, self.E)
+        return FlareFunction.apply(radius, center, t, direction, self)
+
+
+class FlareFunction(torch.autograd.Function):
+    """image = flare(radius, center, coating thickness per element, light direction.xyz)."""
+
+    @staticmethod
+    def forward(ctx, radius, center, thickness, direction, renderer: DifferentiableRenderer):
+        ctx.renderer = renderer
+        ctx.save_for_backward(direction)
+        with torch.no_grad():
+            image = renderer.forward_kernels(radius, center, thickness, direction)
+        return image.clone()
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        (direction,) = ctx.saved_tensors
+        r = ctx.renderer
+        g_radius, g_center, g_thick, g_n = r.backward_kernels(grad_image)
+        # n = normalize(-v), v = direction: dn/dv = -(I - n n^T) / |v|
+        v = direction.to(torch.float64)
+        norm = torch.linalg.norm(v)
+        n = -v / norm
+        g_n = g_n.to(torch.float64)
+        g_v = -(g_n - n * torch.dot(n, g_n)) / norm
+        dt = direction.dtype
+        return (g_radius.to(dt), g_center.to(dt), g_thick.to(dt), g_v.to(dt), None)
