@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument('--ghosts', type=int, default=0, help='keep only the first N ghosts')
     ap.add_argument('--batched-frames', type=int, default=256,
                     help='frames of the batched form measured beside the plain path (0 = skip)')
+    ap.add_argument('--no-differentiable', action='store_true',
+                    help='skip the forward+adjoint measurement of the 16-surface lens')
     ap.add_argument('--raster-stats', action='store_true',
                     help='count k_raster work (statistics build of the library) instead of timing')
     return ap.parse_args()
@@ -531,6 +533,7 @@ def main() -> None:
     if not args.no_e2e:
         e2e = run_e2e(w, args)
     batched = run_batched(args) if args.batched_frames > 0 and rank == 0 else None
+    differentiable = run_differentiable(args) if not args.no_differentiable and rank == 0 else None
 
     peak, peak_kind = load_peaks()
     raster_s = last['raster'] / 1e3
@@ -580,6 +583,7 @@ def main() -> None:
             'clocks': clk,
             'gpu_launches': launches,
             'batched': batched,
+            'differentiable': differentiable,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -698,6 +702,59 @@ def run_batched(args) -> dict:
         'autotune_ms': {k: round(v, 3) for k, v in choice.timings_ms.items()},
         'identical_to_plain': identical,
         'timing': 'wall clock from a synchronised start to a synchronised end; batched = CUDA-graph replays',
+    }
+
+
+def run_differentiable(args) -> dict:
+    """Forward+adjoint against the plain forward on the 16-surface lens at 512^2 (64^2 grid,
+    8 wavelengths, 120 ghosts), gradients with respect to 16 radii, 15 gaps, 16 coating
+    thicknesses and 2 light coordinates; then 200 Adam steps of parameter recovery."""
+    import torch
+
+    from realflare_gb300 import synthetic
+    from realflare_gb300.diff import DifferentiableRenderer
+    from realflare_gb300.recover import recover
+    from realflare_gb300.tasks import GhostApertureTask, GhostTask
+
+    w = synthetic.workload('differentiable-16')
+    p = w.project
+    ghost = GhostTask().run(p, GhostApertureTask().run(p)).tensor
+    r = DifferentiableRenderer(p, ghost)
+    params = [t.clone().requires_grad_(True) for t in r.params.tensors()]
+    target = torch.zeros((p.render.resolution.height(), p.render.resolution.width(), 4), device='cuda')
+
+    def forward():
+        with torch.no_grad():
+            radius, center, t, direction = r.params.elements(*params, r.E)
+            return r.forward_kernels(radius, center, t, direction)
+
+    def forward_adjoint():
+        for q in params:
+            q.grad = None
+        image = r.render(*params)
+        ((image - target)[..., :3] ** 2).sum().backward()
+
+    def timed(fn, n=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n * 1e3
+
+    f_ms = timed(forward)
+    fa_ms = timed(forward_adjoint)
+    rec = recover(p, ghost, steps=200)
+    return {
+        'workload': 'differentiable-16', 'image': '512x512', 'rays': r.n_rays,
+        'parameters': sum(q.numel() for q in params),
+        'forward_ms': f_ms, 'forward_adjoint_ms': fa_ms, 'ratio': fa_ms / f_ms,
+        'recovery': {'steps': rec.steps, 'loss_start': rec.loss_start, 'loss_end': rec.loss_end,
+                     'param_rms_error_start': rec.error_start, 'param_rms_error_end': rec.error_end,
+                     'seconds': rec.seconds},
+        'timing': 'wall clock per iteration (each includes the binning host synchronisation)',
     }
 
 

@@ -618,6 +618,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     float* blend = xyz + 3 * p.maxW * p.WS;
     float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
     float* rgrad = grgb + 96 * kBlocks;                // [record][corner * 5 + attribute]
+    // per-warp transpose buffer of the 20 per-lane products (stride 21: conflict-free)
+    float* red = rgrad + kBatchRecords * 4 * kGradAttrs + (threadIdx.x >> 5) * (32 * 21);
+    __shared__ int next_block;
     const int tile = blockIdx.x;
     const int tx = tile % p.ntx, ty = tile / p.ntx;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -686,10 +689,14 @@ __global__ void __launch_bounds__(kThreads, 2)
             const uint32_t entry = tile_entries[base + j / p.WS];
             finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
         }
+        if (threadIdx.x == 0) next_block = 0;
         __syncthreads();
 #pragma unroll 1
-        for (int k = 0; k < kBlocks / 8; k++) {
-            const int blk = warp + 8 * k;
+        for (;;) {
+            int blk = 0;
+            if (lane == 0) blk = atomicAdd(&next_block, 1);
+            blk = __shfl_sync(0xffffffffu, blk, 0);
+            if (blk >= kBlocks) break;
             const int x0 = tx * T + (blk % kCols) * 8, y0 = ty * T + (blk / kCols) * 4;
             const int px = x0 + (lane & 7), py = y0 + (lane >> 3);
             const int bx0 = x0 * S, by0 = y0 * S, bx1 = bx0 + 8 * S - 1, by1 = by0 + 4 * S - 1;
@@ -743,6 +750,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                                     hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
                         }
                     }
+                    if (!__any_sync(0xffffffffu, hits > 0)) continue;
                     float gw[kGradAttrs] = {0.f, 0.f, 0.f, 0.f, 0.f};
                     float wt[4] = {0.f, 0.f, 0.f, 0.f};
                     if (hits > 0) {
@@ -777,18 +785,20 @@ __global__ void __launch_bounds__(kThreads, 2)
                         gw[3] = ci_raw > 0.0f ? d * gi * ri * ai : 0.0f;
                         gw[4] = ai_raw > 0.0f ? d * gi * ri * ci : 0.0f;
                     }
-                    // the warp's sum of each corner attribute's gradient
+                    // the warp's sum of each corner attribute's gradient: every lane writes its
+                    // 20 products, lane k < 20 adds up column k
 #pragma unroll
-                    for (int c = 0; c < 4; c++) {
+                    for (int c = 0; c < 4; c++)
 #pragma unroll
-                        for (int a = 0; a < kGradAttrs; a++) {
-                            float val = gw[a] * wt[c];
-#pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-                            if (lane == c * kGradAttrs + a && val != 0.0f)
-                                atomicAdd(&rgrad[j * 4 * kGradAttrs + c * kGradAttrs + a], val);
-                        }
+                        for (int a = 0; a < kGradAttrs; a++) red[lane * 21 + c * kGradAttrs + a] = gw[a] * wt[c];
+                    __syncwarp();
+                    if (lane < 4 * kGradAttrs) {
+                        float sum = 0.0f;
+#pragma unroll 8
+                        for (int l = 0; l < 32; l++) sum += red[l * 21 + lane];
+                        if (sum != 0.0f) atomicAdd(&rgrad[j * 4 * kGradAttrs + lane], sum);
                     }
+                    __syncwarp();
                 }
             }
         }
@@ -1063,7 +1073,7 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     p.ntx = (p.width + 31) / 32;
     const int nty = (p.height + 31) / 32;
     const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
-                        sizeof(float) * (96 * 32 + kBatchRecords * 4 * kGradAttrs);
+                        sizeof(float) * (96 * 32 + kBatchRecords * 4 * kGradAttrs + 8 * 32 * 21);
     static std::atomic<size_t> allowed[kMaxDevices];
     RF_TRY(allow_smem(k_raster_backward, smem, allowed));
     k_raster_backward<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries, ghost,
