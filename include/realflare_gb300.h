@@ -355,6 +355,14 @@ int rf_quad_setup_backward(const float* rays, int32_t path_count, int32_t wavele
                            const float* grad_intensities, float* grad_rays, void* stream);
 
 /* ---- compositing ---------------------------------------------------------------------- */
+/* Image-based light accumulation (realflare/api/engine.py:120-150): image (device
+ * float[height][width][4], read and written) += for each light sample k, weights[k][m] *
+ * (frame k mirrored: m = 0 as is, 1 flipped vertically, 2 both ways, 3 horizontally),
+ * per channel, in sample order; then divided by divisor when it is > 0. frames: device
+ * float[count][height][width][4]; weights: device float[count][4][4]. */
+int rf_accumulate_mirrored(const float* frames, const float* weights, int32_t count, int32_t width,
+                           int32_t height, float divisor, float* image, void* stream);
+
 /* out = a * wa + b * wb elementwise over n floats (Engine.flare_starburst,
  * realflare/api/engine.py:174-187, uses wa = 2, wb = 1). */
 int rf_axpby(const float* a, float wa, const float* b, float wb, float* out, int64_t n,

@@ -161,6 +161,7 @@ SIGNATURES = {
     'rf_aperture_dust': [P, I32, I32, F32, F32, F32, F32, F32, F32, F32, F32, P],
     'rf_aperture_noise_dust': [P, P, P, I32, I32, F32, F32, P],
     'rf_axpby': [P, F32, P, F32, P, I64, P],
+    'rf_accumulate_mirrored': [P, P, I32, I32, I32, F32, P, P],
     'rf_trace_adjoint': [P, P, P, ctypes.POINTER(TraceArgs), P, P, P, P],
     'rf_raster_backward': [P, P, P, P, P, ctypes.POINTER(RasterArgs), P, P, P, P],
     'rf_vertex_backward': [P, P, I32, I32, I32, P, P, P, P],

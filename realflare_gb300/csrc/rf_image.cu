@@ -152,6 +152,39 @@ __global__ void __launch_bounds__(256) k_noise_blur(const float* __restrict__ sr
     else image[(size_t)y * w + x] = image[(size_t)y * w + x] * (1.0f - strength * acc);
 }
 
+// Engine.image_flare's accumulation (realflare/api/engine.py:120-150): per light sample i,
+// image += v_i0 * F_i + v_i1 * flip_y(F_i) + v_i2 * flip_yx(F_i) + v_i3 * flip_x(F_i) (per
+// channel weights), in sample order, each product and sum rounded as in float32 numpy;
+// then image /= count. One thread per output pixel (float4).
+__global__ void k_accumulate_mirrored(const float4* __restrict__ frames, const float4* __restrict__ weights, int n,
+                                      int w, int h, float divisor, float4* __restrict__ image) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)w * h) return;
+    const int x = (int)(i % w), y = (int)(i / w);
+    const long long frame = (long long)w * h;
+    const long long src[4] = {(long long)y * w + x, (long long)(h - 1 - y) * w + x,
+                              (long long)(h - 1 - y) * w + (w - 1 - x), (long long)y * w + (w - 1 - x)};
+    float4 acc = image[i];
+    for (int k = 0; k < n; k++) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const float4 f = frames[k * frame + src[m]];
+            const float4 v = weights[4 * k + m];
+            acc.x = __fadd_rn(acc.x, __fmul_rn(v.x, f.x));
+            acc.y = __fadd_rn(acc.y, __fmul_rn(v.y, f.y));
+            acc.z = __fadd_rn(acc.z, __fmul_rn(v.z, f.z));
+            acc.w = __fadd_rn(acc.w, __fmul_rn(v.w, f.w));
+        }
+    }
+    if (divisor > 0.0f) {
+        acc.x = __fdiv_rn(acc.x, divisor);
+        acc.y = __fdiv_rn(acc.y, divisor);
+        acc.z = __fdiv_rn(acc.z, divisor);
+        acc.w = __fdiv_rn(acc.w, divisor);
+    }
+    image[i] = acc;
+}
+
 __global__ void k_axpby(const float* __restrict__ a, float wa, const float* __restrict__ b, float wb,
                         float* __restrict__ out, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,5 +258,16 @@ extern "C" int rf_axpby(const float* a, float wa, const float* b, float wb, floa
     if (!a || !b || !out || n < 0) return RF_ERR_INVALID_ARG;
     if (n == 0) return RF_OK;
     k_axpby<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a, wa, b, wb, out, n);
+    return launch_status();
+}
+
+extern "C" int rf_accumulate_mirrored(const float* frames, const float* weights, int32_t count, int32_t width,
+                                      int32_t height, float divisor, float* image, void* stream) {
+    using namespace rf;
+    if (!frames || !weights || !image || count < 0 || width < 1 || height < 1) return RF_ERR_INVALID_ARG;
+    if (!aligned16(frames) || !aligned16(weights) || !aligned16(image)) return RF_ERR_INVALID_ARG;
+    const long long n = (long long)width * height;
+    k_accumulate_mirrored<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+        (const float4*)frames, (const float4*)weights, count, width, height, divisor, (float4*)image);
     return launch_status();
 }

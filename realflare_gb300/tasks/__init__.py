@@ -13,8 +13,10 @@ command queue). Results stay on the device until ``.array`` is read.
 """
 from __future__ import annotations
 
+import copy
 import ctypes
 import math
+import os
 
 import numpy as np
 import torch
@@ -29,7 +31,7 @@ from .._abi import (
     lib,
 )
 from ..constants import LAMBDA_MID, light_spectrum
-from ..data import Project, RealflareError
+from ..data import Project, QPointF, QSize, RealflareError
 from ..device import Image, Rays, empty, ptr, require_cuda, stream_handle, to_device
 
 
@@ -289,7 +291,128 @@ class StarburstTask(Task):
         return self.starburst(project, aperture)
 
 
+class PreprocessTask(Task):
+    """Ghost culling (``realflare/api/tasks/preprocessing.py:22-103``): a 3 x 3 grid is
+    traced at 1 % of the grid length with the light on axis and one wavelength; each path's
+    "area" is |x| * |x| of its first ray's sensor position (the reference squares x; kept),
+    and the paths with the largest areas are dropped up to ``cull_percentage``. Returns the
+    kept path indexes in increasing-area order (the trace then keeps the paths' order)."""
+
+    def __init__(self, queue=None) -> None:
+        super().__init__(queue)
+        self.raytracing_task = RaytracingTask(queue, cache=False)
+        self._cache = None
+
+    def preprocess(self, project: Project) -> tuple:
+        p = copy.deepcopy(project)
+        r = p.render
+        r.grid_count = 3
+        r.grid_length = project.render.grid_length * 0.01
+        r.resolution = QSize(100, 100)
+        r.wavelength_count = 1
+        r.wavelengths = ()
+        p.flare.light.position = QPointF(0, 0)
+        rays = self.raytracing_task.run(p)
+        if rays is None:
+            return tuple()
+        P, W, R = rays.shape
+        x = rays.tensor[0].view(P, W, R)[:, 0, 0].cpu().numpy()
+        areas = {path: np.abs(x[path]) * np.abs(x[path]) for path in range(P)}
+        sorted_areas = sorted(areas.items(), key=lambda item: item[1])
+        index_to_keep = int(len(sorted_areas) * (1 - project.render.cull_percentage))
+        return tuple(int(k) for k, v in sorted_areas[:index_to_keep])
+
+    def run(self, project: Project) -> tuple:
+        lens, render = project.flare.lens, project.render
+        key = (hash(lens), render.grid_length, render.cull_percentage)
+        if self._cache is None or self._cache[0] != key:
+            self._cache = (key, self.preprocess(project))
+        return self._cache[1]
+
+
+def resize_linear(array: np.ndarray, width: int, height: int) -> np.ndarray:
+    """Bilinear resize with half-pixel centres and clamped edges (the documented behaviour of
+    OpenCV's ``resize`` with ``INTER_LINEAR`` on float images, which the reference calls,
+    ``preprocessing.py:136``): each output pixel interpolates the 2 x 2 nearest inputs."""
+    h0, w0 = array.shape[:2]
+
+    def axis(n_out, n_in):
+        f = (np.arange(n_out, dtype=np.float64) + 0.5) * (n_in / n_out) - 0.5
+        i = np.floor(f).astype(np.int64)
+        t = (f - i).astype(np.float32)
+        t = np.where(i < 0, 0.0, t)
+        i = np.where(i < 0, 0, i)
+        t = np.where(i >= n_in - 1, 0.0, t).astype(np.float32)
+        i = np.minimum(i, n_in - 1)
+        return i, np.minimum(i + 1, n_in - 1), t
+
+    xi0, xi1, xt = axis(width, w0)
+    yi0, yi1, yt = axis(height, h0)
+    a = np.asarray(array, np.float32)
+    rows = a[yi0] * (1 - yt)[:, None, None] + a[yi1] * yt[:, None, None]
+    return (rows[:, xi0] * (1 - xt)[None, :, None] + rows[:, xi1] * xt[None, :, None]).astype(np.float32)
+
+
+class ImageSamplingTask(Task):
+    """Light image samples (``realflare/api/tasks/preprocessing.py:106-185``): the image is
+    resized to ``image_sample_resolution`` (even width, height by the render's aspect ratio,
+    even), and every pixel below the ``1 - samples / pixels`` percentile of its channel mean
+    is zeroed; returns RGBA float32 (alpha 0). Files are ``.npy`` arrays (H, W, 3 or 4) of
+    linear RGB: there is no image decoder in this package."""
+
+    def __init__(self, queue=None) -> None:
+        super().__init__(queue)
+        self._cache = None
+
+    @staticmethod
+    def load_file(path: str) -> np.ndarray:
+        path = os.path.expandvars(path)
+        if not path.endswith('.npy') or not os.path.exists(path):
+            raise RealflareError(f'Invalid Image path for flare light: {path}')
+        array = np.load(path)
+        if array.ndim != 3 or array.shape[2] < 3:
+            raise RealflareError(f'Invalid Image path for flare light: {path}')
+        array = array[..., :3]
+        if array.dtype == np.uint8:
+            array = np.divide(array, 255)
+        return np.float32(array)
+
+    @staticmethod
+    def sample_data(array: np.ndarray, width: int, height: int, samples: int) -> np.ndarray:
+        array = resize_linear(array, width, height)
+        intensity = np.mean(array, axis=2, keepdims=True).ravel()
+        try:
+            threshold = 1 - (samples / len(intensity))
+        except ZeroDivisionError:
+            threshold = 0
+        threshold = np.clip(threshold * 100, 0, 100)
+        percentile = np.percentile(intensity, threshold)
+        mask = intensity > percentile
+        masked = np.reshape(array.copy(), (-1, 3))
+        masked[~mask] = np.zeros((3,), np.float32)
+        masked = masked.reshape(array.shape)
+        return np.dstack((masked, np.zeros(masked.shape[:-1]))).astype(np.float32)
+
+    def run(self, project: Project) -> np.ndarray:
+        light = project.flare.light
+        width = max(light.image_sample_resolution, 1)
+        if width % 2 != 0:
+            width += 1
+        resolution = project.render.resolution
+        ratio = resolution.height() / resolution.width()
+        height = width * ratio
+        if height % 2 != 0:
+            height += 1
+        height = int(height)
+        key = (light.image_file, width, height, light.image_samples)
+        if self._cache is None or self._cache[0] != key:
+            array = self.load_file(light.image_file)
+            self._cache = (key, self.sample_data(array, width, height, light.image_samples))
+        return self._cache[1]
+
+
 __all__ = [
-    'ApertureTask', 'GhostApertureTask', 'GhostTask', 'RasterizingTask', 'RaytracingTask',
+    'ApertureTask', 'GhostApertureTask', 'GhostTask', 'ImageSamplingTask', 'PreprocessTask', 'RasterizingTask',
+    'RaytracingTask',
     'StarburstApertureTask', 'StarburstTask', 'SPECTRUM_WIDTH', 'RF_OK',
 ]

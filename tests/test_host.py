@@ -125,3 +125,25 @@ def test_prepare_arguments():
     p.render.resolution = QSize(100, 50)
     d = lens.direction((0.5, -0.5), p.render.resolution, (36, 24), 50)
     assert list(d) == pytest.approx([9.0, -4.5, 50, 1])
+
+
+def test_light_image_resize_and_sampling():
+    """ImageSamplingTask's host arithmetic (preprocessing.py:126-162): bilinear resize with
+    half-pixel centres and clamped edges, and the percentile mask keeping the brightest."""
+    from realflare_gb300.tasks import ImageSamplingTask, resize_linear
+
+    a = np.arange(4 * 6 * 3, dtype=np.float32).reshape(4, 6, 3)
+    assert np.array_equal(resize_linear(a, 6, 4), a)
+    half = resize_linear(a, 3, 2)
+    # each output pixel is the mean of a 2 x 2 input block at a factor of 2
+    assert np.allclose(half[0, 0], a[0:2, 0:2].mean((0, 1)))
+    up = resize_linear(a, 12, 8)
+    assert np.array_equal(up[0, 0], a[0, 0]) and np.array_equal(up[-1, -1], a[-1, -1])
+    img = np.zeros((8, 8, 3), np.float32)
+    img[1, 2] = 5.0
+    img[6, 6] = 3.0
+    img[3, 3] = 1.0
+    sd = ImageSamplingTask.sample_data(img, 8, 8, 2)
+    assert sd.shape == (8, 8, 4) and np.all(sd[..., 3] == 0)
+    lit = np.argwhere(sd[..., :3].sum(-1) > 0)
+    assert {tuple(v) for v in lit} == {(1, 2), (6, 6)}
