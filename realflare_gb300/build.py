@@ -7,7 +7,10 @@ pointers). Object files go to ``realflare_gb300/_build/``.
 The quad/vertex setup is compiled without fused multiply-add contraction so that its
 outputs equal the oracle's bit for bit; the trace likewise unless RF_TRACE_FMAD=1 (the
 trace's positions then differ from the reference's by a few ulps); every other unit uses
-nvcc's default contraction.
+nvcc's default contraction. The trace, its adjoint and the rasteriser flush denormals
+(-ftz=true): their values are never denormal in practice, and the flag drops the denormal
+handling around reciprocals, square roots and divisions (the trace's outputs stay
+bit-identical).
 """
 from __future__ import annotations
 
@@ -24,16 +27,16 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 UNITS = {
     'rf_api.cu': [],
-    'rf_trace.cu': [] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false'],
+    'rf_trace.cu': ['-ftz=true'] + ([] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false']),
     'rf_quad.cu': ['-fmad=false'],
     'rf_sort.cu': [],
     'rf_bin.cu': [],
-    'rf_raster.cu': [],
+    'rf_raster.cu': ['-ftz=true'],
     'rf_fft.cu': [],
     'rf_image.cu': [],
     'rf_batch.cu': [],
     # the adjoint re-traces rays: it must use the trace's arithmetic
-    'rf_adjoint.cu': [] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false'],
+    'rf_adjoint.cu': ['-ftz=true'] + ([] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false']),
 }
 
 

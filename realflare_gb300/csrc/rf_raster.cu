@@ -205,16 +205,26 @@ __device__ __forceinline__ float ghost_sample(const float* __restrict__ tex, int
     const float fu = floorf(u), fv = floorf(v);
     const float a = u - fu, b = v - fv;
     const int i0 = (int)fu, j0 = (int)fv;
-    const bool i0_in = (unsigned)i0 < (unsigned)w, i1_in = (unsigned)(i0 + 1) < (unsigned)w;
-    const bool j0_in = (unsigned)j0 < (unsigned)h, j1_in = (unsigned)(j0 + 1) < (unsigned)h;
-    // load from clamped (always valid) addresses, then zero the texels outside the image
-    const int ia = min(max(i0, 0), w - 1), ib = min(max(i0 + 1, 0), w - 1);
-    const float* row0 = tex + (size_t)min(max(j0, 0), h - 1) * w;
-    const float* row1 = tex + (size_t)min(max(j0 + 1, 0), h - 1) * w;
-    const float t00 = (i0_in && j0_in) ? __ldg(row0 + ia) : 0.0f;
-    const float t10 = (i1_in && j0_in) ? __ldg(row0 + ib) : 0.0f;
-    const float t01 = (i0_in && j1_in) ? __ldg(row1 + ia) : 0.0f;
-    const float t11 = (i1_in && j1_in) ? __ldg(row1 + ib) : 0.0f;
+    float t00, t10, t01, t11;
+    if ((unsigned)i0 < (unsigned)(w - 1) && (unsigned)j0 < (unsigned)(h - 1)) {
+        // all four texels inside (the common case)
+        const float* q = tex + (j0 * w + i0);
+        t00 = __ldg(q);
+        t10 = __ldg(q + 1);
+        t01 = __ldg(q + w);
+        t11 = __ldg(q + w + 1);
+    } else {
+        const bool i0_in = (unsigned)i0 < (unsigned)w, i1_in = (unsigned)(i0 + 1) < (unsigned)w;
+        const bool j0_in = (unsigned)j0 < (unsigned)h, j1_in = (unsigned)(j0 + 1) < (unsigned)h;
+        // load from clamped (always valid) addresses, then zero the texels outside the image
+        const int ia = min(max(i0, 0), w - 1), ib = min(max(i0 + 1, 0), w - 1);
+        const float* row0 = tex + (size_t)min(max(j0, 0), h - 1) * w;
+        const float* row1 = tex + (size_t)min(max(j0 + 1, 0), h - 1) * w;
+        t00 = (i0_in && j0_in) ? __ldg(row0 + ia) : 0.0f;
+        t10 = (i1_in && j0_in) ? __ldg(row0 + ib) : 0.0f;
+        t01 = (i0_in && j1_in) ? __ldg(row1 + ia) : 0.0f;
+        t11 = (i1_in && j1_in) ? __ldg(row1 + ib) : 0.0f;
+    }
     return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
 }
 
