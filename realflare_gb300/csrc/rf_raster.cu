@@ -42,6 +42,9 @@ namespace {
 #ifndef RF_RASTER_MIN_BLOCKS
 #define RF_RASTER_MIN_BLOCKS 3
 #endif
+#ifndef RF_RASTER_MIN_BLOCKS_S1  // the one-sample kernel needs fewer registers
+#define RF_RASTER_MIN_BLOCKS_S1 4
+#endif
 #ifndef RF_RASTER_CLASSIFY
 #define RF_RASTER_CLASSIFY 1
 #endif
@@ -62,6 +65,7 @@ __device__ unsigned long long g_raster_stats[5];
 
 struct alignas(16) Rec {
     int bb[4];       // xmin, xmax, ymin, ymax (first: read as one 16-byte vector)
+    float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad (16-byte load)
     int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
     int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
     int flags;       // 1: bounds rejection is exact; 2: both triangles collinear (never inside)
@@ -69,7 +73,8 @@ struct alignas(16) Rec {
     float uv[8], rrel[4], inten[4], refl[4];
     float qf[8];     // q as floats (exact: |q| < 2^24)
 };
-static_assert(sizeof(Rec) % 16 == 0 && offsetof(Rec, bb) == 0, "records are read with 16-byte loads");
+static_assert(sizeof(Rec) % 16 == 0 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0,
+              "records are read with 16-byte loads");
 
 struct RasterParams {
     int width, height, T, ntx, S, W, WS, G, maxW;
@@ -153,9 +158,10 @@ __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float
         d[i] = sx[i] * sx[j] + sy[i] * sy[j];
         r2[i] = sx[i] * sx[i] + sy[i] * sy[i];
     }
-    // a_i and r2_i are integers (differences and sums of products of integers), so a product
-    // of the four is 0 exactly when one of them is 0, and otherwise at least 1 and finite
-    const bool rare = (a[0] * a[1]) * (a[2] * a[3]) == 0.0f || (r2[0] * r2[1]) * (r2[2] * r2[3]) == 0.0f;
+    // a_i are integers (differences of products of integers), so their product is 0 exactly
+    // when one of them is 0, and otherwise at least 1 and finite; a vertex on the sample
+    // point (r2_i = 0, s_i = 0) makes a_i and a_{i-1} exactly 0, so it is rare too
+    const bool rare = (a[0] * a[1]) * (a[2] * a[3]) == 0.0f;
     float ir[4], r[4], t[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -293,7 +299,7 @@ __device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t
     r.qf[2 * k + 1] = (float)r.q[2 * k + 1];
 }
 // edges, bounds and flags of a record whose corners are stored
-__device__ __forceinline__ void finish_record(const RasterParams& p, int w, int i, Rec& r) {
+__device__ __forceinline__ void finish_record(const RasterParams& p, int w, int i, const float* xyz, Rec& r) {
     const int* q = r.q;
     edge_coeffs(q[0], q[1], q[2], q[3], r.ec + 0);
     edge_coeffs(q[2], q[3], q[4], q[5], r.ec + 3);
@@ -314,6 +320,15 @@ __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int 
         flags |= 2;
     r.flags = flags;
     r.color = w * p.WS + i;
+    if (p.W > 1) {
+        const float* c = xyz + 3 * r.color;
+        r.col[0] = c[0];
+        r.col[1] = c[1];
+        r.col[2] = c[2];
+    } else {  // rgb += frag (rasterizing.cl:648-650): a weight of exactly 1
+        r.col[0] = r.col[1] = r.col[2] = 1.0f;
+    }
+    r.col[3] = 0.0f;
 }
 
 // A CTA of 8 warps shades one T x T tile (T = 32 or 16): the tile's T^2 / 32 blocks of
@@ -328,8 +343,9 @@ constexpr size_t raster_smem_bytes(int maxW, int WS) {
 }
 
 // Tile (tx, ty), whose entries are tile_entries[begin, end). smem4 holds the dynamic shared
-// memory (raster_smem_bytes), next_block two shared counters.
-template <int T>
+// memory (raster_smem_bytes), next_block two shared counters. kS: the anti-aliasing sample
+// count when known at compile time (1), else 0 (p.S).
+template <int T, int kS>
 __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint32_t begin, uint32_t end,
                                             const uint32_t* __restrict__ tile_entries,
                                             const float* __restrict__ ghost, const float* __restrict__ spectrum,
@@ -364,7 +380,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
         }
     }
 
-    const int S = p.S;
+    const int S = kS ? kS : p.S;
     const FragmentConsts fc = fcs;
     RF_STAT(unsigned long long st_iter = 0; unsigned long long st_whole = 0; unsigned long long st_frag = 0;
             unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0;)
@@ -408,7 +424,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
         for (int h = 0; h < kLoads; h++) {
             const int e = my_entry + 64 * h;
             if (have_next[h])
-                for (int i = my_corner; i < p.WS; i += 4) finish_record(p, next_w[h], i, dst[e * p.WS + i]);
+                for (int i = my_corner; i < p.WS; i += 4) finish_record(p, next_w[h], i, xyz, dst[e * p.WS + i]);
         }
         prefetch(first + per_batch);
     };
@@ -491,17 +507,11 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                     RF_STAT(st_frag++; st_frag_whole += is_whole;)
                     float wt[4];
                     barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
-                    const float f = fragment_fast(r, wt, ghost, p, fc, hits);
-                    if (p.W > 1) {
-                        const float* c = xyz + 3 * r.color;
-                        r0 += c[0] * f;
-                        r1 += c[1] * f;
-                        r2 += c[2] * f;
-                    } else {
-                        r0 += f;
-                        r1 += f;
-                        r2 += f;
-                    }
+                    const float f = fragment_fast(r, wt, ghost, p, fc, kS == 1 ? 1 : hits);
+                    const float4 col = *reinterpret_cast<const float4*>(r.col);
+                    r0 += col.x * f;
+                    r1 += col.y * f;
+                    r2 += col.z * f;
                 }
             }
             acc[(3 * blk) * 32 + lane] = r0;
@@ -533,15 +543,15 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
 }
 
 // One CTA per tile of a frame.
-template <int T>
-__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
+template <int T, int kS>
+__global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : RF_RASTER_MIN_BLOCKS)
     k_raster(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
              const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
              const float* __restrict__ spectrum, RasterParams p, FragmentConsts fcs, float4* __restrict__ image) {
     extern __shared__ float4 smem4[];
     __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
     const int tile = blockIdx.x;
-    raster_tile<T>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs, image,
+    raster_tile<T, kS>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs, image,
                    tile % p.ntx, tile / p.ntx, smem4, next_block);
 }
 
@@ -575,7 +585,7 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
         p.ntx = (p.width + T - 1) / T;
         const FragmentConsts fc = fragment_consts(p);
         const int tile = gt - fr.tile_offset;
-        raster_tile<T>(vtx_all + 2 * fr.vertex_offset, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
+        raster_tile<T, 0>(vtx_all + 2 * fr.vertex_offset, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
                        ghosts + fr.ghost_offset, spectrum, p, fc, images + fr.image_offset, tile % p.ntx,
                        tile / p.ntx, smem4, next_block);
         __syncthreads();  // the tile's accumulators and `item` are free again
@@ -697,7 +707,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         __syncthreads();
         for (int j = threadIdx.x; j < n_rec; j += kThreads) {
             const uint32_t entry = tile_entries[base + j / p.WS];
-            finish_record(p, (int)(entry % p.maxW), j % p.WS, recs[j]);
+            finish_record(p, (int)(entry % p.maxW), j % p.WS, xyz, recs[j]);
         }
         if (threadIdx.x == 0) next_block = 0;
         __syncthreads();
@@ -958,18 +968,25 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
     return RF_OK;
 }
 
-template <int T>
-int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
-                  const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
+template <int T, int kS>
+int launch_raster_s(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
+                    const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
     static std::atomic<size_t> allowed[kMaxDevices];
     p.T = T;
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
     const size_t smem = raster_smem_bytes<T>(p.maxW, p.WS);
-    RF_TRY(allow_smem(k_raster<T>, smem, allowed));
-    k_raster<T><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum, p,
-                                                   fragment_consts(p), (float4*)image);
+    RF_TRY(allow_smem(k_raster<T, kS>, smem, allowed));
+    k_raster<T, kS><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum,
+                                                       p, fragment_consts(p), (float4*)image);
     return launch_status();
+}
+
+template <int T>
+int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
+                  const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
+    if (p.S == 1) return launch_raster_s<T, 1>(vertexes, offsets, entries, ghost, spectrum, p, image, s);
+    return launch_raster_s<T, 0>(vertexes, offsets, entries, ghost, spectrum, p, image, s);
 }
 
 template <int T>
