@@ -274,6 +274,8 @@ typedef struct rf_batch_sizes {
     int64_t trace_blocks, quad_blocks, vertex_blocks, pair_blocks;
     int64_t image_pixels, ghost_floats;
     int32_t max_colors, max_sub;  /* largest max(W-1,1) * WS and WS over the frames */
+    int32_t max_sub_steps;        /* largest anti-aliasing sample count over the frames */
+    int32_t pad;
 } rf_batch_sizes;
 
 /* Checks every frame and fills the derived fields of frames (host memory) and sizes.

@@ -132,6 +132,8 @@ class BatchSizes(ctypes.Structure):
         ('ghost_floats', ctypes.c_int64),
         ('max_colors', ctypes.c_int32),
         ('max_sub', ctypes.c_int32),
+        ('max_sub_steps', ctypes.c_int32),
+        ('pad', ctypes.c_int32),
     ]
 
 

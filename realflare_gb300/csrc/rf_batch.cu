@@ -89,6 +89,7 @@ extern "C" int rf_batch_plan(rf_frame* frames, int32_t frame_count, int32_t tile
         const int colors = (int)maxW * f.raster.wavelength_sub_count;
         if (colors > z.max_colors) z.max_colors = colors;
         if (f.raster.wavelength_sub_count > z.max_sub) z.max_sub = f.raster.wavelength_sub_count;
+        if (f.raster.sub_steps > z.max_sub_steps) z.max_sub_steps = f.raster.sub_steps;
         // normalize(direction.xyz * -1) in FP32, the value rf_trace computes (this file is
         // compiled without floating-point contraction too)
         const float vx = -f.trace.direction[0], vy = -f.trace.direction[1], vz = -f.trace.direction[2];

@@ -560,8 +560,8 @@ __host__ __device__ inline FragmentConsts fragment_consts(const RasterParams& p)
 
 // Every frame of a batch in one persistent launch: each CTA takes the next tile from the
 // queue (tiles ordered by decreasing entry count) until none are left.
-template <int T>
-__global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
+template <int T, int kS>
+__global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : RF_RASTER_MIN_BLOCKS)
     k_raster_batch(const rf_frame* __restrict__ frames, int F, int tiles, const uint32_t* __restrict__ order,
                    unsigned* __restrict__ queue, const unsigned long long* __restrict__ entry_total,
                    long long capacity, const float4* __restrict__ vtx_all, const uint32_t* __restrict__ tile_offsets,
@@ -569,25 +569,38 @@ __global__ void __launch_bounds__(kThreads, RF_RASTER_MIN_BLOCKS)
                    const float* __restrict__ spectrum, float4* __restrict__ images) {
     extern __shared__ float4 smem4[];
     __shared__ int next_block[2];
-    __shared__ int item;
+    // the current tile's frame settings, held in shared memory rather than registers
+    __shared__ RasterParams sp;
+    __shared__ FragmentConsts sfc;
+    __shared__ int item, s_tile, s_gt;
+    __shared__ long long s_vtx, s_ghost, s_image;
     if (*entry_total > (unsigned long long)capacity) return;  // incomplete lists: nothing is drawn
     for (;;) {
-        if (threadIdx.x == 0) item = (int)atomicAdd(queue, 1u);
+        if (threadIdx.x == 0) {
+            item = (int)atomicAdd(queue, 1u);
+            if (item < tiles) {
+                const int gt = (int)order[item];
+                const int f = find_frame(frames, F, gt, [](const rf_frame& fr) { return fr.tile_offset; });
+                const rf_frame& fr = frames[f];
+                RasterParams q;
+                make_params(fr.raster, q);
+                q.T = T;
+                q.ntx = (q.width + T - 1) / T;
+                sp = q;
+                sfc = fragment_consts(q);
+                s_gt = gt;
+                s_tile = gt - fr.tile_offset;
+                s_vtx = fr.vertex_offset;
+                s_ghost = fr.ghost_offset;
+                s_image = fr.image_offset;
+            }
+        }
         __syncthreads();
-        const int it = item;
-        if (it >= tiles) break;
-        const int gt = (int)order[it];
-        const int f = find_frame(frames, F, gt, [](const rf_frame& fr) { return fr.tile_offset; });
-        const rf_frame& fr = frames[f];
-        RasterParams p;
-        make_params(fr.raster, p);
-        p.T = T;
-        p.ntx = (p.width + T - 1) / T;
-        const FragmentConsts fc = fragment_consts(p);
-        const int tile = gt - fr.tile_offset;
-        raster_tile<T, 0>(vtx_all + 2 * fr.vertex_offset, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
-                       ghosts + fr.ghost_offset, spectrum, p, fc, images + fr.image_offset, tile % p.ntx,
-                       tile / p.ntx, smem4, next_block);
+        if (item >= tiles) break;
+        const int gt = s_gt, tile = s_tile;
+        raster_tile<T, kS>(vtx_all + 2 * s_vtx, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
+                           ghosts + s_ghost, spectrum, sp, sfc, images + s_image, tile % sp.ntx, tile / sp.ntx, smem4,
+                           next_block);
         __syncthreads();  // the tile's accumulators and `item` are free again
     }
 }
@@ -625,7 +638,8 @@ __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6}
 // corners interpolate. Per record the warp sums its pixels' contributions with shuffles;
 // the CTA sums warps in shared memory and adds each record's totals to the two vertices
 // (wavelength pair endpoints) of each corner once per tile.
-__global__ void __launch_bounds__(kThreads, 2)
+template <int kS>
+__global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     k_raster_backward(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
                       const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
                       const float* __restrict__ spectrum, RasterParams p, FragmentConsts fc,
@@ -688,7 +702,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     for (int i = threadIdx.x; i < kBatchRecords * 4 * kGradAttrs; i += kThreads) rgrad[i] = 0.0f;
 
-    const int S = p.S;
+    const int S = kS ? kS : p.S;
     const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
     const int per_batch = kBatchRecords / p.WS;
     const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
@@ -989,7 +1003,7 @@ int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t
     return launch_raster_s<T, 0>(vertexes, offsets, entries, ghost, spectrum, p, image, s);
 }
 
-template <int T>
+template <int T, int kS>
 int launch_raster_batch(const rf_frame* frames, const rf_batch_sizes& z, const float* vertexes,
                         const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
                         const float* spectrum, const BatchWorkspace& w, long long capacity,
@@ -999,19 +1013,20 @@ int launch_raster_batch(const rf_frame* frames, const rf_batch_sizes& z, const f
     // the largest frame layout: 3 * max(W-1,1) * WS colours, WS blend weights (rounded to 4)
     const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * z.max_colors + ((z.max_sub + 3) & ~3)) +
                         sizeof(float) * 96 * (T * T / 32);
-    RF_TRY(allow_smem(k_raster_batch<T>, smem, allowed));
+    RF_TRY(allow_smem(k_raster_batch<T, kS>, smem, allowed));
     int dev = 0, sms = 0;
     RF_TRY(cuda_status(cudaGetDevice(&dev)));
     RF_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)));
     int per_sm = ctas_per_sm[dev].load();
     if (per_sm == 0) {
-        RF_TRY(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_batch<T>, kThreads, smem)));
+        RF_TRY(cuda_status(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_batch<T, kS>, kThreads, smem)));
         per_sm = per_sm > 0 ? per_sm : 1;
         ctas_per_sm[dev].store(per_sm);
     }
     const long long ctas = std::min<long long>((long long)sms * per_sm, z.tiles);
     RF_TRY(cuda_status(cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), s)));
-    k_raster_batch<T><<<(unsigned)ctas, kThreads, smem, s>>>(
+    k_raster_batch<T, kS><<<(unsigned)ctas, kThreads, smem, s>>>(
         frames, z.frame_count, z.tiles, batch_tile_order(w, z), w.queue, (const unsigned long long*)entry_total,
         capacity, (const float4*)vertexes, tile_offsets, tile_entries, ghosts, spectrum, (float4*)images);
     return launch_status();
@@ -1034,13 +1049,19 @@ extern "C" int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* siz
     if (z.max_sub < 1 || z.max_sub > kBatchRecords || z.max_colors > 4096) return RF_ERR_INVALID_ARG;
     BatchWorkspace w = batch_layout((char*)workspace, z, entry_capacity);
     if (w.bytes > workspace_bytes) return RF_ERR_INVALID_ARG;
+    const bool one = z.max_sub_steps <= 1;  // every frame takes one sample per pixel
+    cudaStream_t s = (cudaStream_t)stream;
     switch (z.tile_size) {
         case 32:
-            return launch_raster_batch<32>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum, w,
-                                           entry_capacity, entry_total, images, (cudaStream_t)stream);
+            return one ? launch_raster_batch<32, 1>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
+                                                    w, entry_capacity, entry_total, images, s)
+                       : launch_raster_batch<32, 0>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
+                                                    w, entry_capacity, entry_total, images, s);
         case 16:
-            return launch_raster_batch<16>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum, w,
-                                           entry_capacity, entry_total, images, (cudaStream_t)stream);
+            return one ? launch_raster_batch<16, 1>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
+                                                    w, entry_capacity, entry_total, images, s)
+                       : launch_raster_batch<16, 0>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
+                                                    w, entry_capacity, entry_total, images, s);
         default:
             return RF_ERR_NOT_SUPPORTED;
     }
@@ -1101,11 +1122,20 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     const int nty = (p.height + 31) / 32;
     const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
                         sizeof(float) * (96 * 32 + kBatchRecords * 4 * kGradAttrs + 8 * 32 * 21);
-    static std::atomic<size_t> allowed[kMaxDevices];
-    RF_TRY(allow_smem(k_raster_backward, smem, allowed));
-    k_raster_backward<<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries, ghost,
-                                                         spectrum, p, fragment_consts(p), (const float4*)image,
-                                                         (const float4*)grad_image, grad_vertexes);
+    static std::atomic<size_t> allowed1[kMaxDevices], allowed0[kMaxDevices];
+    if (p.S == 1) {
+        RF_TRY(allow_smem(k_raster_backward<1>, smem, allowed1));
+        k_raster_backward<1><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                                ghost, spectrum, p, fragment_consts(p),
+                                                                (const float4*)image, (const float4*)grad_image,
+                                                                grad_vertexes);
+    } else {
+        RF_TRY(allow_smem(k_raster_backward<0>, smem, allowed0));
+        k_raster_backward<0><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                                ghost, spectrum, p, fragment_consts(p),
+                                                                (const float4*)image, (const float4*)grad_image,
+                                                                grad_vertexes);
+    }
     return launch_status();
 }
 
