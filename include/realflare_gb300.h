@@ -332,7 +332,7 @@ int rf_trace_adjoint(const rf_lens_element* elements, const int32_t* paths, cons
                      const rf_trace_args* args, const float* grad_rays, float* grad_elements,
                      float* grad_direction, void* stream);
 
-/* Adjoint of rf_raster (32 x 32 tiles; the same tile lists). Coverage and the mean-value
+/* Adjoint of rf_raster (the same tile size and tile lists). Coverage and the mean-value
  * weights depend on the vertex positions only through integer sample coordinates, so they
  * are held fixed: the gradient flows to each vertex's interpolated attributes (aperture
  * position, rrel, reflectance, intensity), not to its screen position (the change of

@@ -60,14 +60,14 @@ __device__ __forceinline__ D3 dsqrt(D3 a) {
 
 // the Fresnel formulas of rf_trace_core.cuh over duals (theta in tangent 0, the coating
 // thicknesses in tangents 1 and 2)
-__device__ D3 fresnel_d(D3 theta0, float n1, float n2) {
+__device__ __noinline__ D3 fresnel_d(D3 theta0, float n1, float n2) {
     D3 theta1 = dasin(dsin(theta0) * n1 / n2);
     D3 cosi = dcos(theta0), cost = dcos(theta1);
     D3 rs = (cosi * n1 - cost * n2) / (cosi * n1 + cost * n2);
     D3 rp = (cost * n1 - cosi * n2) / (cost * n1 + cosi * n2);
     return (rs * rs + rp * rp) / 2.0f;
 }
-__device__ D3 fresnel_ar_d(D3 theta0, float lambda, D3 d1, float n0, float n1, float n2) {
+__device__ __noinline__ D3 fresnel_ar_d(D3 theta0, float lambda, D3 d1, float n0, float n1, float n2) {
     D3 s0 = dsin(theta0);
     D3 theta1 = dasin(s0 * n0 / n1);
     D3 theta2 = dasin(s0 * n0 / n2);
@@ -104,7 +104,8 @@ __device__ D3 stack_r2_d(D3 r01, D3 r12, D3 r23, D3 d1, D3 d2) {
     D3 bre = dconst(1.0f) + r01 * ere, bim = r01 * eim;
     return (tre * tre + tim * tim) / (bre * bre + bim * bim);
 }
-__device__ D3 fresnel_two_layer_d(D3 theta0, float lambda, float n0, float na, D3 da, float nb, D3 db, float n2) {
+__device__ __noinline__ D3 fresnel_two_layer_d(D3 theta0, float lambda, float n0, float na, D3 da, float nb, D3 db,
+                                           float n2) {
     D3 s0 = dsin(theta0), c0 = dcos(theta0);
     D3 sa = s0 * (n0 / na), sb = s0 * (n0 / nb), s2 = s0 * (n0 / n2);
     D3 ca = dsqrt(dconst(1.0f) - sa * sa), cb = dsqrt(dconst(1.0f) - sb * sb), c2 = dsqrt(dconst(1.0f) - s2 * s2);
@@ -121,8 +122,7 @@ __device__ D3 fresnel_two_layer_d(D3 theta0, float lambda, float n0, float na, D
 // ---------------------------------------------------------------- recording
 struct Step {
     float px, py, pz, dx, dy, dz;
-    int lens;
-    int reflect;  // 1 when the ray reflects at this element
+    int tag;  // element index | 1 << 16 when the ray reflects at this element
 };
 struct StepRecorder {
     Step* steps;
@@ -130,7 +130,7 @@ struct StepRecorder {
     int argmax;  // step whose |xy| / height is the final rrel
     float best;
     __device__ __forceinline__ void step(int lens, float px, float py, float pz, float dx, float dy, float dz) {
-        if (n < kAdjMaxSteps) steps[n] = {px, py, pz, dx, dy, dz, lens, 0};
+        if (n < kAdjMaxSteps) steps[n] = {px, py, pz, dx, dy, dz, lens};
         n++;
     }
     __device__ __forceinline__ void rrel(float r, float) {
@@ -140,7 +140,7 @@ struct StepRecorder {
         }
     }
     __device__ __forceinline__ void reflect() {
-        if (n - 1 < kAdjMaxSteps) steps[n - 1].reflect = 1;
+        if (n - 1 < kAdjMaxSteps) steps[n - 1].tag |= 1 << 16;
     }
 };
 
@@ -251,174 +251,195 @@ __global__ void __launch_bounds__(kAdjThreads) k_trace_adjoint(const rf_lens_ele
     for (int i = threadIdx.x; i < E * kGradPerElement + 3; i += kAdjThreads) acc[i] = 0.0f;
     __syncthreads();
 
-    float gE[kAdjMaxElements * kGradPerElement];
+    const int lane = threadIdx.x & 31;
+    // every lane runs the reverse sweep (lanes without a valid ray add zeros), so that the
+    // warp can sum each step's gradient with shuffles when its rays share one ghost path
+    // and wavelength (the same element sequence); otherwise lanes add to shared memory
+    const long long idx_raw = first + threadIdx.x;
+    const bool in_range = idx_raw < p.n_rays;
+    const long long idx = in_range ? idx_raw : first;
+    const long long n = p.n_rays;
+    const int ray_id = (int)(idx % p.R);
+    const long long pw = idx / p.R;
+    const int wl_id = (int)(pw % p.W);
+    const int path_id = (int)(pw / p.W);
+    const int row = (int)((pw - pw_first) % p.W);
+    const float* ior_row = table ? ior_tab + row * E : nullptr;
+    const float wavelength = __ldg(wavelengths + wl_id);
+    const float* coef_base = &elements[0].coefficients[0];
+    auto ior_of = [&](int el) -> float {
+        if (ior_row) return ior_row[el];
+        float nn = se[el].ior;
+        if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
+        return nn;
+    };
+    TraceFrame f;
+    f.E = E;
+    f.aperture = p.aperture;
+    f.W = p.W;
+    f.G = p.G;
+    f.R = p.R;
+    f.cmin = p.cmin;
+    f.layer_n0 = p.layer_n0;
+    f.layer_n1 = p.layer_n1;
+    f.dir[0] = p.dir[0];
+    f.dir[1] = p.dir[1];
+    f.dir[2] = p.dir[2];
+    const int gy = (int)truncf((float)ray_id / (float)p.G);
+    const int gx = ray_id - gy * p.G;
+    // a ray whose outputs have no gradient contributes nothing: it is not re-traced
+    float g_out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool needed = false;
+    if (in_range) {
 #pragma unroll
-    for (int i = 0; i < kAdjMaxElements * kGradPerElement; i++) gE[i] = 0.0f;
-    V3 gdir = v3(0.0f, 0.0f, 0.0f);
-
-    const long long idx = first + threadIdx.x;
-    if (idx < p.n_rays) {
-        const long long n = p.n_rays;
-        const float g_out[6] = {grad_rays[idx], grad_rays[n + idx], grad_rays[2 * n + idx],
-                                grad_rays[3 * n + idx], grad_rays[4 * n + idx], grad_rays[5 * n + idx]};
-        const int ray_id = (int)(idx % p.R);
-        const long long pw = idx / p.R;
-        const int wl_id = (int)(pw % p.W);
-        const int path_id = (int)(pw / p.W);
-        const int row = (int)((pw - pw_first) % p.W);
-        const float* ior_row = table ? ior_tab + row * E : nullptr;
-        const float wavelength = __ldg(wavelengths + wl_id);
-        const float* coef_base = &elements[0].coefficients[0];
-        auto ior_of = [&](int el) -> float {
-            if (ior_row) return ior_row[el];
-            float nn = se[el].ior;
-            if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
-            return nn;
-        };
-        TraceFrame f;
-        f.E = E;
-        f.aperture = p.aperture;
-        f.W = p.W;
-        f.G = p.G;
-        f.R = p.R;
-        f.cmin = p.cmin;
-        f.layer_n0 = p.layer_n0;
-        f.layer_n1 = p.layer_n1;
-        f.dir[0] = p.dir[0];
-        f.dir[1] = p.dir[1];
-        f.dir[2] = p.dir[2];
-        const int gy = (int)truncf((float)ray_id / (float)p.G);
-        const int gx = ray_id - gy * p.G;
-        Step steps[kAdjMaxSteps];
-        StepRecorder rec{steps, 0, -1, 0.0f};
-        float out[6];
-        trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
-                      f, out, rec);
-        const bool valid = !isnan(out[5]) && rec.n <= kAdjMaxSteps && rec.n > 0;
-        if (valid) {
-            const float refl = out[5];
-            // adjoint of the state leaving the current step: position and direction
-            V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);
-            bool apt_pending = true;  // the last aperture crossing sets pos_apt
-            for (int j = rec.n - 1; j >= 0; j--) {
-                const Step& st = steps[j];
-                const int i = st.lens;
-                const SmemElement& e = se[i];
-                const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
-                const Hit h = intersect(pin.x, pin.y, pin.z, din.x, din.y, din.z, e);
-                V3 gh = gp;  // adjoint of the hit point
-                V3 gn = v3(0.0f, 0.0f, 0.0f);
-                V3 gdin = v3(0.0f, 0.0f, 0.0f);
-                if (j == rec.n - 1) gh = gh + v3(g_out[0], g_out[1], 0.0f);  // sensor position
-                if (i == p.aperture) {
-                    if (apt_pending) {
-                        gh.x += g_out[2] / e.height;
-                        gh.y += g_out[3] / e.height;
-                        apt_pending = false;
-                    }
-                    gdin = gd;  // no change of direction at the stop
-                } else {
-                    if (j == rec.argmax) {
-                        const float rxy = sqrtf(h.px * h.px + h.py * h.py);
-                        if (rxy > 0.0f) {
-                            const float s = g_out[4] / (rxy * e.height);
-                            gh.x += s * h.px;
-                            gh.y += s * h.py;
-                        }
-                    }
-                    const V3 nrm = v3(h.nx, h.ny, h.nz);
-                    if (i == E - 1) {
-                        gdin = gd;
-                    } else {
-                        const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
-                        const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
-                        const float n2 = ior_of(i);
-                        if (st.reflect) {
-                            // d' = d - 2 (d.n) n
-                            const float dn = dot(din, nrm), gdn = dot(gd, nrm);
-                            gdin = gd - nrm * (2.0f * gdn);
-                            gn = gn - (gd * dn + din * gdn) * 2.0f;
-                            // reflectance factor R(theta, thicknesses), refl *= R when R > 0
-                            const float c = -dn;
-                            const float cc = clampf(c, -1.0f, 1.0f);
-                            const float incident = acosf(cc);
-                            const float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
-                            D3 th = {theta, 1.0f, 0.0f, 0.0f};
-                            D3 R;
-                            float gtheta = 0.0f;
-                            if (e.layers == 2) {
-                                R = fresnel_two_layer_d(th, wavelength, n1, p.layer_n0, D3{e.d0, 0.f, 1.f, 0.f},
-                                                        p.layer_n1, D3{e.d1, 0.f, 0.f, 1.f}, n2);
-                            } else if (e.layers == 1 || e.coating > 0) {
-                                const float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
-                                const D3 d1 = e.layers == 1 ? D3{e.d0, 0.f, 1.f, 0.f}
-                                                            : dconst((float)e.coating / (4.0f * nc));
-                                R = fresnel_ar_d(th, wavelength, d1, n1, nc, n2);
-                            } else {
-                                R = fresnel_d(th, n1, n2);
-                            }
-                            if (R.v > 0.0f) {
-                                const float gR = g_out[5] * refl / R.v;
-                                gtheta = gR * R.g0;
-                                gE[i * kGradPerElement + 2] += gR * R.g1;
-                                gE[i * kGradPerElement + 3] += gR * R.g2;
-                            }
-                            if (fabsf(c) < 1.0f) {
-                                const float gc = gtheta * (-rsqrtf(1.0f - c * c));
-                                // c = -d.n
-                                gdin = gdin - nrm * gc;
-                                gn = gn - din * gc;
-                            }
-                        } else {
-                            // d' = o d + k n, k = o c - sqrt(1 - o^2 (1 - c^2)), c = -d.n
-                            const float o = n1 / n2;
-                            const float c = -dot(din, nrm);
-                            const float sint2 = (o * o) * (1.0f - c * c);
-                            const float sq = sqrtf(fabsf(1.0f - sint2));
-                            const float k = o * c - sq;
-                            const float gk = dot(gd, nrm);
-                            const float dk_dc = sq > 0.0f ? o - o * o * c / sq : o;
-                            gdin = gd * o - nrm * (gk * dk_dc);
-                            gn = gn + gd * k - din * (gk * dk_dc);
-                        }
-                    }
-                }
-                V3 gpin = v3(0.0f, 0.0f, 0.0f);
-                float gr = 0.0f, gc = 0.0f;
-                intersect_adjoint(pin, din, e, gh, gn, gpin, gdin, gr, gc);
-                gE[i * kGradPerElement + 0] += gr;
-                gE[i * kGradPerElement + 1] += gc;
-                gp = gpin;
-                gd = gdin;
-            }
-            // entry ray: p_in = hit0 - dir, d_in = dir; hit0 = grid point hitting element 0
-            gdir = gdir + gd - gp;
-            const V3 g0 = v3(p.grid[gx], -p.grid[gy], 1.0f);
-            const Hit h0 = intersect(g0.x, g0.y, g0.z, 0.0f, 0.0f, -1.0f, se[0]);
-            if (h0.hit) {
-                V3 gpg = v3(0.f, 0.f, 0.f), gdg = v3(0.f, 0.f, 0.f);
-                float gr = 0.0f, gc = 0.0f;
-                intersect_adjoint(g0, v3(0.0f, 0.0f, -1.0f), se[0], gp, v3(0.f, 0.f, 0.f), gpg, gdg, gr, gc);
-                gE[0] += gr;
-                gE[1] += gc;
-            }
+        for (int k = 0; k < 6; k++) {
+            g_out[k] = grad_rays[k * n + idx];
+            needed = needed || g_out[k] != 0.0f;
         }
     }
-    // warp sums, then one shared-memory add per warp and value, then global
-    const int lane = threadIdx.x & 31;
-    for (int i = 0; i < E * kGradPerElement; i++) {
-        float v = gE[i];
+    Step steps[kAdjMaxSteps];
+    StepRecorder rec{steps, 0, -1, 0.0f};
+    float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (needed)
+        trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
+                      f, out, rec);
+    const bool valid = needed && !isnan(out[5]) && rec.n <= kAdjMaxSteps && rec.n > 0;
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    const int leader = vmask ? __ffs(vmask) - 1 : 0;
+    const int key = path_id * p.W + wl_id;
+    const int lead_key = __shfl_sync(0xffffffffu, key, leader);  // every lane takes part
+    const bool uniform = __all_sync(0xffffffffu, !valid || key == lead_key);
+    const int n_steps = __reduce_max_sync(0xffffffffu, valid ? (unsigned)rec.n : 0u);
+    const float refl = out[5];
+    V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);  // adjoint of the state leaving a step
+    bool apt_pending = true;  // the last aperture crossing sets pos_apt
+    for (int j = n_steps - 1; j >= 0; j--) {
+        float g4[kGradPerElement] = {0.f, 0.f, 0.f, 0.f};
+        int el = 0;
+        if (valid && j < rec.n) {
+            const Step& st = steps[j];
+            const int i = st.tag & 0xffff;
+            el = i;
+            const SmemElement& e = se[i];
+            const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
+            const Hit h = intersect(pin.x, pin.y, pin.z, din.x, din.y, din.z, e);
+            V3 gh = gp;  // adjoint of the hit point
+            V3 gn = v3(0.0f, 0.0f, 0.0f);
+            V3 gdin = v3(0.0f, 0.0f, 0.0f);
+            if (j == rec.n - 1) gh = gh + v3(g_out[0], g_out[1], 0.0f);  // sensor position
+            if (i == p.aperture) {
+                if (apt_pending) {
+                    gh.x += g_out[2] / e.height;
+                    gh.y += g_out[3] / e.height;
+                    apt_pending = false;
+                }
+                gdin = gd;  // no change of direction at the stop
+            } else {
+                if (j == rec.argmax) {
+                    const float rxy = sqrtf(h.px * h.px + h.py * h.py);
+                    if (rxy > 0.0f) {
+                        const float sc = g_out[4] / (rxy * e.height);
+                        gh.x += sc * h.px;
+                        gh.y += sc * h.py;
+                    }
+                }
+                const V3 nrm = v3(h.nx, h.ny, h.nz);
+                if (i == E - 1) {
+                    gdin = gd;
+                } else {
+                    const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
+                    const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
+                    const float n2 = ior_of(i);
+                    if (st.tag >> 16) {
+                        // d' = d - 2 (d.n) n
+                        const float dn = dot(din, nrm), gdn = dot(gd, nrm);
+                        gdin = gd - nrm * (2.0f * gdn);
+                        gn = gn - (gd * dn + din * gdn) * 2.0f;
+                        // reflectance factor R(theta, thicknesses), refl *= R when R > 0
+                        const float c = -dn;
+                        const float cc = clampf(c, -1.0f, 1.0f);
+                        const float incident = acosf(cc);
+                        const float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
+                        D3 th = {theta, 1.0f, 0.0f, 0.0f};
+                        D3 R;
+                        float gtheta = 0.0f;
+                        if (e.layers == 2) {
+                            R = fresnel_two_layer_d(th, wavelength, n1, p.layer_n0, D3{e.d0, 0.f, 1.f, 0.f},
+                                                    p.layer_n1, D3{e.d1, 0.f, 0.f, 1.f}, n2);
+                        } else if (e.layers == 1 || e.coating > 0) {
+                            const float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
+                            const D3 d1 = e.layers == 1 ? D3{e.d0, 0.f, 1.f, 0.f}
+                                                        : dconst((float)e.coating / (4.0f * nc));
+                            R = fresnel_ar_d(th, wavelength, d1, n1, nc, n2);
+                        } else {
+                            R = fresnel_d(th, n1, n2);
+                        }
+                        if (R.v > 0.0f) {
+                            const float gR = g_out[5] * refl / R.v;
+                            gtheta = gR * R.g0;
+                            g4[2] += gR * R.g1;
+                            g4[3] += gR * R.g2;
+                        }
+                        if (fabsf(c) < 1.0f) {
+                            const float gc = gtheta * (-rsqrtf(1.0f - c * c));
+                            // c = -d.n
+                            gdin = gdin - nrm * gc;
+                            gn = gn - din * gc;
+                        }
+                    } else {
+                        // d' = o d + k n, k = o c - sqrt(1 - o^2 (1 - c^2)), c = -d.n
+                        const float o = n1 / n2;
+                        const float c = -dot(din, nrm);
+                        const float sint2 = (o * o) * (1.0f - c * c);
+                        const float sq = sqrtf(fabsf(1.0f - sint2));
+                        const float k = o * c - sq;
+                        const float gk = dot(gd, nrm);
+                        const float dk_dc = sq > 0.0f ? o - o * o * c / sq : o;
+                        gdin = gd * o - nrm * (gk * dk_dc);
+                        gn = gn + gd * k - din * (gk * dk_dc);
+                    }
+                }
+            }
+            V3 gpin = v3(0.0f, 0.0f, 0.0f);
+            intersect_adjoint(pin, din, e, gh, gn, gpin, gdin, g4[0], g4[1]);
+            gp = gpin;
+            gd = gdin;
+        }
+        if (uniform) {
+            el = __shfl_sync(0xffffffffu, el, leader);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0 && v != 0.0f) atomicAdd(&acc[i], v);
+            for (int k = 0; k < kGradPerElement; k++) {
+                float v = g4[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0 && v != 0.0f) atomicAdd(&acc[el * kGradPerElement + k], v);
+            }
+        } else if (valid && j < rec.n) {
+#pragma unroll
+            for (int k = 0; k < kGradPerElement; k++)
+                if (g4[k] != 0.0f) atomicAdd(&acc[el * kGradPerElement + k], g4[k]);
+        }
     }
-    float dv[3] = {gdir.x, gdir.y, gdir.z};
+    // entry ray: p_in = hit0 - dir, d_in = dir; hit0 = grid point hitting element 0
+    V3 gdir = v3(0.0f, 0.0f, 0.0f);
+    float g0r = 0.0f, g0c = 0.0f;
+    if (valid) {
+        gdir = gd - gp;
+        const V3 g0 = v3(p.grid[gx], -p.grid[gy], 1.0f);
+        const Hit h0 = intersect(g0.x, g0.y, g0.z, 0.0f, 0.0f, -1.0f, se[0]);
+        if (h0.hit) {
+            V3 gpg = v3(0.f, 0.f, 0.f), gdg = v3(0.f, 0.f, 0.f);
+            intersect_adjoint(g0, v3(0.0f, 0.0f, -1.0f), se[0], gp, v3(0.f, 0.f, 0.f), gpg, gdg, g0r, g0c);
+        }
+    }
+    const float tail[5] = {g0r, g0c, gdir.x, gdir.y, gdir.z};
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        float v = dv[k];
+    for (int k = 0; k < 5; k++) {
+        float v = tail[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0 && v != 0.0f) atomicAdd(&acc[E * kGradPerElement + k], v);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0f)
+            atomicAdd(&acc[k < 2 ? k : E * kGradPerElement + (k - 2)], v);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < E * kGradPerElement; i += kAdjThreads)

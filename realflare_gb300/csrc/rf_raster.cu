@@ -632,20 +632,20 @@ constexpr int kGradAttrs = 5;  // per corner: u, v, rrel, reflectance, intensity
 // vertex float of each attribute (pos.xy, uv.xy, rrel, reflectance, intensity, pad)
 __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6};
 
-// Backward of k_raster for 32 x 32 tiles: the same tiles, entry lists, records, coverage
+// Backward of k_raster (32 x 32 or 16 x 16 tiles): the same tiles, entry lists, records, coverage
 // and mean-value weights as the forward (held fixed: they are piecewise constant in the
 // vertex positions), differentiating each fragment with respect to the attributes its
 // corners interpolate. Per record the warp sums its pixels' contributions with shuffles;
 // the CTA sums warps in shared memory and adds each record's totals to the two vertices
 // (wavelength pair endpoints) of each corner once per tile.
-template <int kS>
+template <int T, int kS>
 __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     k_raster_backward(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
                       const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
                       const float* __restrict__ spectrum, RasterParams p, FragmentConsts fc,
                       const float4* __restrict__ image, const float4* __restrict__ grad_image,
                       float* __restrict__ grad_vtx) {
-    constexpr int T = 32, kBlocks = 32, kCols = 4;
+    constexpr int kBlocks = T * T / 32, kCols = T / 8;
     extern __shared__ float4 smem4[];
     Rec* recs = (Rec*)smem4;
     float* xyz = (float*)(recs + kBatchRecords);
@@ -1112,29 +1112,40 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     RasterParams p;
     if (!make_params(*args, p)) return RF_ERR_INVALID_ARG;
     if (p.WS > kBatchRecords || p.maxW * p.WS > 4096) return RF_ERR_INVALID_ARG;
-    if (tile_size_of(*args) != 32) return RF_ERR_NOT_SUPPORTED;
+    const int T = tile_size_of(*args);
+    if (T != 32 && T != 16) return RF_ERR_NOT_SUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     const long long n_vertices = (long long)args->path_count * args->grid_count * args->grid_count *
                                  args->wavelength_count + 1;
     RF_TRY(cuda_status(cudaMemsetAsync(grad_vertexes, 0, sizeof(float) * 8 * (size_t)n_vertices, s)));
-    p.T = 32;
-    p.ntx = (p.width + 31) / 32;
-    const int nty = (p.height + 31) / 32;
+    p.T = T;
+    p.ntx = (p.width + T - 1) / T;
+    const int nty = (p.height + T - 1) / T;
     const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
-                        sizeof(float) * (96 * 32 + kBatchRecords * 4 * kGradAttrs + 8 * 32 * 21);
-    static std::atomic<size_t> allowed1[kMaxDevices], allowed0[kMaxDevices];
-    if (p.S == 1) {
-        RF_TRY(allow_smem(k_raster_backward<1>, smem, allowed1));
-        k_raster_backward<1><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                                ghost, spectrum, p, fragment_consts(p),
-                                                                (const float4*)image, (const float4*)grad_image,
-                                                                grad_vertexes);
+                        sizeof(float) * (96 * (T * T / 32) + kBatchRecords * 4 * kGradAttrs + 8 * 32 * 21);
+    const FragmentConsts fc = fragment_consts(p);
+    const float4 *im = (const float4*)image, *gim = (const float4*)grad_image;
+    const unsigned grid = (unsigned)(p.ntx * nty);
+    if (T == 32 && p.S == 1) {
+        static std::atomic<size_t> allowed[kMaxDevices];
+        RF_TRY(allow_smem(k_raster_backward<32, 1>, smem, allowed));
+        k_raster_backward<32, 1><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+    } else if (T == 32) {
+        static std::atomic<size_t> allowed[kMaxDevices];
+        RF_TRY(allow_smem(k_raster_backward<32, 0>, smem, allowed));
+        k_raster_backward<32, 0><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+    } else if (p.S == 1) {
+        static std::atomic<size_t> allowed[kMaxDevices];
+        RF_TRY(allow_smem(k_raster_backward<16, 1>, smem, allowed));
+        k_raster_backward<16, 1><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
     } else {
-        RF_TRY(allow_smem(k_raster_backward<0>, smem, allowed0));
-        k_raster_backward<0><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                                ghost, spectrum, p, fragment_consts(p),
-                                                                (const float4*)image, (const float4*)grad_image,
-                                                                grad_vertexes);
+        static std::atomic<size_t> allowed[kMaxDevices];
+        RF_TRY(allow_smem(k_raster_backward<16, 0>, smem, allowed));
+        k_raster_backward<16, 0><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
+                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
     }
     return launch_status();
 }

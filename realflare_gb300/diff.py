@@ -145,7 +145,8 @@ class DifferentiableRenderer:
         self.P, self.W, self.G = a.path_count, a.wavelength_count, a.grid_count
         self.n_rays = ti.ray_count
         self.area, self.min_area = prepare.quad_constants(project)
-        self.raster_args = prepare.raster_args(project, self.P, self.W, tuple(ghost.shape[:2]), tile_size=32)
+        # 16-pixel tiles: a 512^2 image has 1024 of them, enough CTAs to fill the GPU
+        self.raster_args = prepare.raster_args(project, self.P, self.W, tuple(ghost.shape[:2]), tile_size=16)
         self.task = RasterizingTask(self.stream)
         self.rays = empty((6, max(self.n_rays, 1)))
         self.params = LensParameters(project, dev)
