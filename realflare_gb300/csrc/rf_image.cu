@@ -13,9 +13,25 @@ namespace rf {
 namespace {
 
 __device__ __forceinline__ float fract1(float x) { return fminf(x - floorf(x), 0x1.fffffep-1f); }
+// sin(x) for the noise hash. The hash's arguments reach 10^6, where sinf takes its slow
+// reduction path; here x is reduced by pi/2 with the Cody-Waite method (W. J. Cody and
+// W. Waite, Software Manual for the Elementary Functions, 1980) using a three-part split of
+// pi/2 (C1 = fl(pi/2), C2 = fl(pi/2 - C1), C3 = fl(pi/2 - C1 - C2), which sum to pi/2 within
+// 1e-23, computed in 200-bit arithmetic) and fused multiply-adds, then sin or cos of the
+// remainder (|r| <= pi/4 + a rounding) by quadrant. Accurate to a few ulps for |x| < 2^22.
+__device__ __forceinline__ float hash_sin(float x) {
+    const float k = rintf(x * 0x1.45f306p-1f);  // x * 2 / pi
+    float r = fmaf(-k, 0x1.921fb6p+0f, x);
+    r = fmaf(-k, -0x1.777a5cp-25f, r);
+    r = fmaf(-k, -0x1.ee59dap-50f, r);
+    float sr, cr;
+    sincosf(r, &sr, &cr);
+    const int q = (int)k & 3;
+    return q == 0 ? sr : (q == 1 ? cr : (q == 2 ? -sr : -cr));
+}
 // noise(x, y, z) of noise.cl:1-5
 __device__ __forceinline__ float noise3(float x, float y, float z) {
-    return fract1(sinf(x * 112.9898f + y * 179.233f + z * 237.212f) * 43758.5453f);
+    return fract1(hash_sin(x * 112.9898f + y * 179.233f + z * 237.212f) * 43758.5453f);
 }
 __device__ __forceinline__ void ndc_of(int px, int py, int w, int h, float& nx, float& ny) {
     nx = 2.0f * ((float)px / (float)(w - 1)) - 1.0f;

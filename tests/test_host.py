@@ -147,3 +147,30 @@ def test_light_image_resize_and_sampling():
     assert sd.shape == (8, 8, 4) and np.all(sd[..., 3] == 0)
     lit = np.argwhere(sd[..., :3].sum(-1) > 0)
     assert {tuple(v) for v in lit} == {(1, 2), (6, 6)}
+
+
+def test_hash_sine_reduction():
+    """The noise hash's sine (rf_image.cu hash_sin): Cody-Waite reduction by pi/2 with the
+    three-part split in the kernel, emulated exactly here (float32 values, fused
+    multiply-adds through float64), then the quadrant; against sin in float64."""
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-2.0**22, 2.0**22, 20000), rng.uniform(-10, 10, 2000),
+                        np.float64(np.arange(-50, 50)) * np.pi / 2]).astype(np.float32)
+    f = np.float32
+    c1, c2, c3 = f(float.fromhex('0x1.921fb6p+0')), f(float.fromhex('-0x1.777a5cp-25')), f(float.fromhex('-0x1.ee59dap-50'))
+
+    def fma(a, b, c):  # exact for these operands: the product fits in 48 bits
+        return (np.float64(a) * np.float64(b) + np.float64(c)).astype(np.float32)
+
+    k = np.rint(x * f(float.fromhex('0x1.45f306p-1'))).astype(np.float32)
+    r = fma(-k, c1, x)
+    r = fma(-k, c2, r)
+    r = fma(-k, c3, r)
+    q = k.astype(np.int64) & 3
+    rs, rc = np.sin(np.float64(r)), np.cos(np.float64(r))
+    got = np.select([q == 0, q == 1, q == 2], [rs, rc, -rs], -rc)
+    want = np.sin(np.float64(x))
+    # x * 2/pi rounds in float32 (a quarter unit at |x| ~ 2^22), so k can be one off and
+    # |r| reach 3 pi/4; sincosf stays accurate there, only the quadrant has to match k
+    assert np.abs(np.float64(r)).max() < 3 * np.pi / 4
+    assert np.abs(got - want).max() < 4e-7
