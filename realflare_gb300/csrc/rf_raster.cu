@@ -63,18 +63,26 @@ __device__ unsigned long long g_raster_stats[5];
 #define RF_STAT(stmt)
 #endif
 
+// Every group the shading loop reads starts on a 16-byte boundary and is read with
+// 16-byte shared-memory loads (ec[12..14] and flags as one vector).
 struct alignas(16) Rec {
-    int bb[4];       // xmin, xmax, ymin, ymax (first: read as one 16-byte vector)
-    float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad (16-byte load)
-    int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
+    int bb[4];       // xmin, xmax, ymin, ymax
+    float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad
+    float qf[8];     // q as floats (exact: |q| < 2^24)
+    float uv[8];     // ghost texture coordinates (u0, v0, ..., u3, v3)
+    float rrel[4], inten[4], refl[4];
     int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
     int flags;       // 1: bounds rejection is exact; 2: both triangles collinear (never inside)
+    int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
     int color;       // w * WS + i
-    float uv[8], rrel[4], inten[4], refl[4];
-    float qf[8];     // q as floats (exact: |q| < 2^24)
 };
-static_assert(sizeof(Rec) % 16 == 0 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0,
+static_assert(sizeof(Rec) == 256 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0 &&
+                  offsetof(Rec, qf) % 16 == 0 && offsetof(Rec, uv) % 16 == 0 && offsetof(Rec, rrel) % 16 == 0 &&
+                  offsetof(Rec, inten) % 16 == 0 && offsetof(Rec, refl) % 16 == 0 &&
+                  offsetof(Rec, ec) % 16 == 0 && offsetof(Rec, flags) == offsetof(Rec, ec) + 15 * sizeof(int),
               "records are read with 16-byte loads");
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ int4 ld4i(const int* p) { return *reinterpret_cast<const int4*>(p); }
 
 struct RasterParams {
     int width, height, T, ntx, S, W, WS, G, maxW;
@@ -101,9 +109,17 @@ __device__ __forceinline__ void edge_coeffs(int ax, int ay, int bx, int by, int*
     e[2] = wadd(wsub(wmul(dy, ax), wmul(A, ay)), top_left(ax, ay, bx, by) ? 0 : -1);
 }
 
+// the 15 edge coefficients and the flags word, by four 16-byte loads
+__device__ __forceinline__ void load_edges(const Rec& r, int e[16]) {
+    const int4 a = ld4i(r.ec), b = ld4i(r.ec + 4), c = ld4i(r.ec + 8), d = ld4i(r.ec + 12);
+    e[0] = a.x, e[1] = a.y, e[2] = a.z, e[3] = a.w, e[4] = b.x, e[5] = b.y, e[6] = b.z, e[7] = b.w;
+    e[8] = c.x, e[9] = c.y, e[10] = c.z, e[11] = c.w, e[12] = d.x, e[13] = d.y, e[14] = d.z, e[15] = d.w;
+}
+
 // intersect_quad (rasterizing.cl:55-93) from plane coefficients
 __device__ __forceinline__ bool inside(const Rec& r, int px, int py) {
-    const int* e = r.ec;
+    int e[16];
+    load_edges(r, e);
     const bool w01 = wadd(wadd(wmul(e[0], py), wmul(e[1], px)), e[2]) >= 0;
     const bool w12 = wadd(wadd(wmul(e[3], py), wmul(e[4], px)), e[5]) >= 0;
     const bool w23 = wadd(wadd(wmul(e[6], py), wmul(e[7], px)), e[8]) >= 0;
@@ -146,11 +162,9 @@ __device__ __forceinline__ int rect_coverage(const Rec& r, int x0, int x1, int y
 // reciprocal-square-root instructions (a few ulps).
 __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float py, float w[4]) {
     float sx[4], sy[4], a[4], d[4], r2[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        sx[i] = rec.qf[2 * i] - px;
-        sy[i] = rec.qf[2 * i + 1] - py;
-    }
+    const float4 q01 = ld4(rec.qf), q23 = ld4(rec.qf + 4);
+    sx[0] = q01.x - px, sy[0] = q01.y - py, sx[1] = q01.z - px, sy[1] = q01.w - py;
+    sx[2] = q23.x - px, sy[2] = q23.y - py, sx[3] = q23.z - px, sy[3] = q23.w - py;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const int j = (i + 1) & 3;
@@ -241,15 +255,18 @@ struct FragmentConsts {
 };
 __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], const float* __restrict__ ghost,
                                                const RasterParams& p, const FragmentConsts& fc, int hits) {
-    const float u = w[0] * r.uv[0] + w[1] * r.uv[2] + w[2] * r.uv[4] + w[3] * r.uv[6];
-    const float v = w[0] * r.uv[1] + w[1] * r.uv[3] + w[2] * r.uv[5] + w[3] * r.uv[7];
+    const float4 uv01 = ld4(r.uv), uv23 = ld4(r.uv + 4);
+    const float u = w[0] * uv01.x + w[1] * uv01.z + w[2] * uv23.x + w[3] * uv23.z;
+    const float v = w[0] * uv01.y + w[1] * uv01.w + w[2] * uv23.y + w[3] * uv23.w;
     const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox, v * fc.tsy + fc.toy);
-    const float rr = w[0] * r.rrel[0] + w[1] * r.rrel[1] + w[2] * r.rrel[2] + w[3] * r.rrel[3];
+    const float4 rl = ld4(r.rrel);
+    const float rr = w[0] * rl.x + w[1] * rl.y + w[2] * rl.z + w[3] * rl.w;
     // smoothstep(1, 0.95, rr) with the division by the constant (0.95 - 1) as a product
     const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
     const float ri = st * st * (3.0f - 2.0f * st);
-    float ai = w[0] * r.inten[0] + w[1] * r.inten[1] + w[2] * r.inten[2] + w[3] * r.inten[3];
-    float ci = w[0] * r.refl[0] + w[1] * r.refl[1] + w[2] * r.refl[2] + w[3] * r.refl[3];
+    const float4 in = ld4(r.inten), rf = ld4(r.refl);
+    float ai = w[0] * in.x + w[1] * in.y + w[2] * in.z + w[3] * in.w;
+    float ci = w[0] * rf.x + w[1] * rf.y + w[2] * rf.z + w[3] * rf.w;
     ai = fmaxf(ai, 0.0f);
     ci = fmaxf(ci, 0.0f);
     return gi * ri * ai * ci * (float)hits;
@@ -796,20 +813,21 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         } else {
                             dLdf = g0 + g1 + g2;
                         }
-                        const float u = wt[0] * r.uv[0] + wt[1] * r.uv[2] + wt[2] * r.uv[4] + wt[3] * r.uv[6];
-                        const float v = wt[0] * r.uv[1] + wt[1] * r.uv[3] + wt[2] * r.uv[5] + wt[3] * r.uv[7];
+                        const float4 uv01 = ld4(r.uv), uv23 = ld4(r.uv + 4);
+                        const float u = wt[0] * uv01.x + wt[1] * uv01.z + wt[2] * uv23.x + wt[3] * uv23.z;
+                        const float v = wt[0] * uv01.y + wt[1] * uv01.w + wt[2] * uv23.y + wt[3] * uv23.w;
                         float dgu, dgv;
                         const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox,
                                                            v * fc.tsy + fc.toy, dgu, dgv);
-                        const float rr = wt[0] * r.rrel[0] + wt[1] * r.rrel[1] + wt[2] * r.rrel[2] + wt[3] * r.rrel[3];
+                        const float4 rl = ld4(r.rrel);
+                        const float rr = wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w;
                         const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
                         const float ri = st * st * (3.0f - 2.0f * st);
                         const float dri = (st > 0.0f && st < 1.0f) ? 6.0f * st * (1.0f - st) * (1.0f / (0.95f - 1.0f))
                                                                   : 0.0f;
-                        const float ai_raw = wt[0] * r.inten[0] + wt[1] * r.inten[1] + wt[2] * r.inten[2] +
-                                             wt[3] * r.inten[3];
-                        const float ci_raw = wt[0] * r.refl[0] + wt[1] * r.refl[1] + wt[2] * r.refl[2] +
-                                             wt[3] * r.refl[3];
+                        const float4 in = ld4(r.inten), rf = ld4(r.refl);
+                        const float ai_raw = wt[0] * in.x + wt[1] * in.y + wt[2] * in.z + wt[3] * in.w;
+                        const float ci_raw = wt[0] * rf.x + wt[1] * rf.y + wt[2] * rf.z + wt[3] * rf.w;
                         const float ai = fmaxf(ai_raw, 0.0f), ci = fmaxf(ci_raw, 0.0f);
                         const float H = (float)hits;
                         const float d = dLdf * H;
