@@ -72,7 +72,7 @@ struct alignas(16) Rec {
     float uv[8];     // ghost texture coordinates (u0, v0, ..., u3, v3)
     float rrel[4], inten[4], refl[4];
     int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
-    int flags;       // 1: bounds rejection is exact; 2: both triangles collinear (never inside)
+    int flags;       // 1: bounds rejection is exact; 2: adds nothing (collinear, or zero_record)
     int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
     int color;       // w * WS + i
 };
@@ -315,6 +315,38 @@ __device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t
     r.qf[2 * k] = (float)r.q[2 * k];
     r.qf[2 * k + 1] = (float)r.q[2 * k + 1];
 }
+// Whether every fragment of a record is zero, so that shading it adds nothing:
+//  - a corner's reflectance is NaN (a ray that failed, at either wavelength of the pair):
+//    the coating term max(NaN, 0) is 0 (rasterizing.cl:495-497) and every other factor is
+//    finite, so each fragment is exactly 0;
+//  - one sample per pixel, every corner's rrel >= 1 (the ray left the lens housing) and the
+//    quad strictly convex and counter-clockwise in sample space, with coordinates that keep
+//    the edge functions exact and an extent below 4096: a covered pixel is then inside the
+//    quad or on one of its edges or corners, where every cross product a_i is >= 0 (an
+//    exact integer) and the tangents share its sign, so the mean-value weights are
+//    non-negative up to rounding and their rrel is >= 1; smoothstep(1, 0.95, rrel) is 0
+//    there, and at most a few units in the last place of 1 below it (a factor below 1e-9).
+// Clockwise quads are left in: on an edge the reference divides by +1e-3 whatever the
+// orientation, so the weights there mix signs.
+__device__ __forceinline__ bool zero_record(const RasterParams& p, const Rec& r, bool safe) {
+    const float4 rf = ld4(r.refl);
+    if (isnan(rf.x) || isnan(rf.y) || isnan(rf.z) || isnan(rf.w)) return true;
+    if (p.S != 1 || !safe || r.bb[1] - r.bb[0] >= 4096 || r.bb[3] - r.bb[2] >= 4096) return false;
+    const float4 rl = ld4(r.rrel);
+    if (!(rl.x >= 1.0f && rl.y >= 1.0f && rl.z >= 1.0f && rl.w >= 1.0f)) return false;
+    const int* q = r.q;
+    bool convex = true;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int j = (i + 1) & 3, k = (i + 2) & 3;
+        // |differences| < 4096: the products are exact in 32 bits
+        const int turn = (q[2 * j] - q[2 * i]) * (q[2 * k + 1] - q[2 * j + 1]) -
+                         (q[2 * j + 1] - q[2 * i + 1]) * (q[2 * k] - q[2 * j]);
+        convex = convex && turn > 0;
+    }
+    return convex;
+}
+
 // edges, bounds and flags of a record whose corners are stored
 __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int i, const float* xyz, Rec& r) {
     const int* q = r.q;
@@ -335,6 +367,7 @@ __device__ __forceinline__ void finish_record(const RasterParams& p, int w, int 
     int flags = safe ? 1 : 0;
     if (edge_i(q[0], q[1], q[2], q[3], q[4], q[5]) == 0 && edge_i(q[0], q[1], q[4], q[5], q[6], q[7]) == 0)
         flags |= 2;
+    if (!(flags & 2) && zero_record(p, r, safe)) flags |= 2;
     r.flags = flags;
     r.color = w * p.WS + i;
     if (p.W > 1) {
@@ -482,7 +515,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                 if (j < n_rec) {
                     const Rec& r = recs[j];
                     const int flags = r.flags;
-                    if (!(flags & 2)) {  // both triangles collinear: intersect_quad rejects all
+                    if (!(flags & 2)) {  // collinear (intersect_quad rejects all) or all-zero
                         const int4 bb = *reinterpret_cast<const int4*>(r.bb);
                         take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);
 #if RF_RASTER_CLASSIFY

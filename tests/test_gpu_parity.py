@@ -199,6 +199,39 @@ def test_raster_matches_oracle(oracle, key, tile):
     assert np.all(got[..., 3] == 0)
 
 
+@pytest.mark.parametrize('key', ['plain-8', 'production-24-small'])
+def test_raster_skipped_records_add_nothing(oracle, key):
+    """The raster leaves out records whose fragments are all zero (a NaN reflectance; or,
+    at one sample per pixel, a convex counter-clockwise quad with every rrel >= 1). With
+    rrel raised by 0.5 (many quads outside the housing) and NaN planted in 3 % of the
+    reflectances, its image still equals the oracle's, which shades every record."""
+    w = workload(key)
+    ghost = ghost_texture()
+    spec = light_spectrum()
+    r = oracle_pipeline(oracle, w, ghost, spec)
+    ra = r['raster_args']
+    assert ra.sub_steps == 1
+    vtx = r['vtx'].copy().reshape(-1, 8)
+    n = vtx.shape[0] - 1  # the last slot stays zero
+    vtx[:n, 4] += 0.5
+    rng = np.random.default_rng(1)
+    vtx[:n, 5][rng.random(n) < 0.03] = np.nan
+    vtx = vtx.reshape(r['vtx'].shape)
+    image_ref = oracle.raster(vtx, r['masks'], ghost, spec, ra)
+    vtx_d = dev(vtx)
+    offsets, entries, task = gpu_tiles(ra, dev(r['bounds']), vtx_d)
+    image = torch.empty((ra.height, ra.width, 4), device='cuda')
+    ghost_d, spec_d = dev(ghost), dev(spec)
+    check(lib().rf_raster(vtx_d.data_ptr(), offsets.data_ptr(), entries.data_ptr(), ghost_d.data_ptr(),
+                          spec_d.data_ptr(), ctypes.byref(ra), image.data_ptr(), stream()), 'rf_raster')
+    torch.cuda.synchronize()
+    got = image.cpu().numpy()
+    assert np.abs(image_ref).sum() > 0
+    # quads outside the housing still light pixels through their negative weights
+    assert ((got[..., :3] != 0).any(-1) == (image_ref[..., :3] != 0).any(-1)).mean() > 0.9999
+    assert rel_l2(got, image_ref) < STAGE_RTOL
+
+
 @pytest.mark.parametrize('key', list(WORKLOADS))
 def test_render_path_matches_oracle(oracle, key):
     """The whole GPU path (trace -> setup -> bin -> raster) against the oracle's."""
