@@ -249,10 +249,12 @@ class GpuFrame:
         ev.append(self._ev())
         with self.torch.cuda.stream(self.stream):
             offsets, entries = raster.bin(self.ra, bounds, vtx)
+            order = raster.order(offsets)
         self.entries = raster.last_entry_count
         ev.append(self._ev())
-        check(L.rf_raster(vtx.data_ptr(), offsets.data_ptr(), entries.data_ptr(), self.ghost.data_ptr(),
-                          self.spectrum_tex.data_ptr(), ctypes.byref(self.ra), self.flare.data_ptr(), s), 'raster')
+        check(L.rf_raster_ordered(vtx.data_ptr(), offsets.data_ptr(), entries.data_ptr(), order.data_ptr(),
+                                  self.ghost.data_ptr(), self.spectrum_tex.data_ptr(), ctypes.byref(self.ra),
+                                  self.flare.data_ptr(), s), 'raster')
         ev.append(self._ev())
         # starburst: aperture (shape x blurred dust), spectrum, compositor
         sa = p.flare.starburst_aperture

@@ -163,6 +163,22 @@ int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_
               const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
               void* stream);
 
+/* Largest-first tile order for rf_raster_ordered: a stable sort of the tiles by decreasing
+ * entry count (to 3 significant bits), from rf_bin_tiles' tile_offsets [tile_count + 1].
+ * tile_order: device uint32[tile_count], a permutation of 0 .. tile_count - 1. Extends the
+ * reference's row-major bin launch (rasterizing.py:257-285) with a work order; the image
+ * does not depend on it. */
+int rf_tile_order_workspace_size(int32_t tile_count, size_t* bytes);
+int rf_tile_order(const uint32_t* tile_offsets, int32_t tile_count, void* workspace,
+                  size_t workspace_bytes, uint32_t* tile_order, void* stream);
+
+/* rf_raster with the tiles started in tile_order (a permutation of the tiles, e.g. from
+ * rf_tile_order) instead of row-major order: heavy tiles first shorten the end of the
+ * launch. The image equals rf_raster's bit for bit. */
+int rf_raster_ordered(const float* vertexes, const uint32_t* tile_offsets,
+                      const uint32_t* tile_entries, const uint32_t* tile_order, const float* ghost,
+                      const float* spectrum, const rf_raster_args* args, float* image, void* stream);
+
 /* Reference-order rasteriser over reference-layout masks (for parity checks). */
 int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_count,
                     const float* ghost, const float* spectrum, const rf_raster_args* args,

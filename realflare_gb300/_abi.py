@@ -153,6 +153,9 @@ SIGNATURES = {
                      ctypes.POINTER(ctypes.c_int64), P],
     'rf_raster_tiles': [ctypes.POINTER(RasterArgs), ctypes.POINTER(I32), ctypes.POINTER(I32)],
     'rf_raster': [P, P, P, P, P, ctypes.POINTER(RasterArgs), P, P],
+    'rf_tile_order_workspace_size': [I32, ctypes.POINTER(ctypes.c_size_t)],
+    'rf_tile_order': [P, I32, P, ctypes.c_size_t, P, P],
+    'rf_raster_ordered': [P, P, P, P, P, P, ctypes.POINTER(RasterArgs), P, P],
     'rf_raster_masks': [P, P, I32, P, P, ctypes.POINTER(RasterArgs), P, P],
     'rf_fft2': [P, P, I32, I32, I32, I32, F32, P],
     'rf_starburst_spectrum': [P, I32, I32, ctypes.POINTER(F32), I32, F32, P, P, P],

@@ -592,15 +592,18 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
     }
 }
 
-// One CTA per tile of a frame.
+// One CTA per tile of a frame: CTA k shades tile order[k], or tile k without an order.
+// CTAs start in index order as slots free up, so an order by decreasing work starts the
+// heaviest tiles first and ends the launch with light ones.
 template <int T, int kS>
 __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : RF_RASTER_MIN_BLOCKS)
     k_raster(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
-             const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
-             const float* __restrict__ spectrum, RasterParams p, FragmentConsts fcs, float4* __restrict__ image) {
+             const uint32_t* __restrict__ tile_entries, const uint32_t* __restrict__ order,
+             const float* __restrict__ ghost, const float* __restrict__ spectrum, RasterParams p, FragmentConsts fcs,
+             float4* __restrict__ image) {
     extern __shared__ float4 smem4[];
     __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
-    const int tile = blockIdx.x;
+    const int tile = order ? (int)order[blockIdx.x] : (int)blockIdx.x;
     raster_tile<T, kS>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs, image,
                    tile % p.ntx, tile / p.ntx, smem4, next_block);
 }
@@ -1034,24 +1037,24 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
 }
 
 template <int T, int kS>
-int launch_raster_s(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
-                    const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
+int launch_raster_s(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const uint32_t* order,
+                    const float* ghost, const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
     static std::atomic<size_t> allowed[kMaxDevices];
     p.T = T;
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
     const size_t smem = raster_smem_bytes<T>(p.maxW, p.WS);
     RF_TRY(allow_smem(k_raster<T, kS>, smem, allowed));
-    k_raster<T, kS><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, ghost, spectrum,
-                                                       p, fragment_consts(p), (float4*)image);
+    k_raster<T, kS><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, order, ghost,
+                                                       spectrum, p, fragment_consts(p), (float4*)image);
     return launch_status();
 }
 
 template <int T>
-int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const float* ghost,
-                  const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
-    if (p.S == 1) return launch_raster_s<T, 1>(vertexes, offsets, entries, ghost, spectrum, p, image, s);
-    return launch_raster_s<T, 0>(vertexes, offsets, entries, ghost, spectrum, p, image, s);
+int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const uint32_t* order,
+                  const float* ghost, const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
+    if (p.S == 1) return launch_raster_s<T, 1>(vertexes, offsets, entries, order, ghost, spectrum, p, image, s);
+    return launch_raster_s<T, 0>(vertexes, offsets, entries, order, ghost, spectrum, p, image, s);
 }
 
 template <int T, int kS>
@@ -1118,9 +1121,10 @@ extern "C" int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* siz
     }
 }
 
-extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
-                         const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
-                         void* stream) {
+namespace {
+int raster_entry(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                 const uint32_t* tile_order, const float* ghost, const float* spectrum, const rf_raster_args* args,
+                 float* image, void* stream) {
     using namespace rf;
     if (!vertexes || !tile_offsets || !ghost || !spectrum || !args || !image) return RF_ERR_INVALID_ARG;
     if (!aligned16(vertexes) || !aligned16(image)) return RF_ERR_INVALID_ARG;
@@ -1129,14 +1133,28 @@ extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, co
     if (p.WS > kBatchRecords || p.maxW * p.WS > 4096) return RF_ERR_INVALID_ARG;
     switch (tile_size_of(*args)) {
         case 32:
-            return launch_raster<32>(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image,
+            return launch_raster<32>(vertexes, tile_offsets, tile_entries, tile_order, ghost, spectrum, p, image,
                                      (cudaStream_t)stream);
         case 16:
-            return launch_raster<16>(vertexes, tile_offsets, tile_entries, ghost, spectrum, p, image,
+            return launch_raster<16>(vertexes, tile_offsets, tile_entries, tile_order, ghost, spectrum, p, image,
                                      (cudaStream_t)stream);
         default:
             return RF_ERR_NOT_SUPPORTED;
     }
+}
+}  // namespace
+
+extern "C" int rf_raster(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                         const float* ghost, const float* spectrum, const rf_raster_args* args, float* image,
+                         void* stream) {
+    return raster_entry(vertexes, tile_offsets, tile_entries, nullptr, ghost, spectrum, args, image, stream);
+}
+
+extern "C" int rf_raster_ordered(const float* vertexes, const uint32_t* tile_offsets, const uint32_t* tile_entries,
+                                 const uint32_t* tile_order, const float* ghost, const float* spectrum,
+                                 const rf_raster_args* args, float* image, void* stream) {
+    if (!tile_order) return RF_ERR_INVALID_ARG;
+    return raster_entry(vertexes, tile_offsets, tile_entries, tile_order, ghost, spectrum, args, image, stream);
 }
 
 extern "C" int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_count, const float* ghost,

@@ -148,6 +148,17 @@ class RasterizingTask(Task):
             return offsets, entries
         raise RealflareError('rf_bin_tiles: workspace did not converge')
 
+    def order(self, offsets):
+        """Tiles by decreasing entry count (rf_tile_order), for rf_raster_ordered."""
+        tiles = offsets.numel() - 1
+        ws_bytes = ctypes.c_size_t()
+        check(self.lib.rf_tile_order_workspace_size(tiles, ctypes.byref(ws_bytes)), 'rf_tile_order_workspace_size')
+        ws = self._buffer('order_workspace', (ws_bytes.value + 3) // 4, torch.int32)
+        order = self._buffer('tile_order', tiles, torch.int32)
+        check(self.lib.rf_tile_order(ptr(offsets), tiles, ptr(ws), ws.numel() * 4, ptr(order), self.stream),
+              'rf_tile_order')
+        return order
+
     def rasterize(self, project: Project, rays: Rays | None, ghost: Image) -> Image:
         render = project.render
         h, w = render.resolution.height(), render.resolution.width()
@@ -160,8 +171,10 @@ class RasterizingTask(Task):
         a = prepare.raster_args(project, P, W, tuple(gt.shape[:2]))
         bounds, inten, vertexes = self.setup(project, rays)
         offsets, entries = self.bin(a, bounds, vertexes)
-        check(self.lib.rf_raster(ptr(vertexes), ptr(offsets), ptr(entries), ptr(gt), ptr(self.spectrum()),
-                                 ctypes.byref(a), ptr(image), self.stream), 'rf_raster')
+        order = self.order(offsets)
+        check(self.lib.rf_raster_ordered(ptr(vertexes), ptr(offsets), ptr(entries), ptr(order), ptr(gt),
+                                         ptr(self.spectrum()), ctypes.byref(a), ptr(image), self.stream),
+              'rf_raster_ordered')
         return Image(tensor=image, args=(rays.args, ghost.args, hash(render), hash(project.flare.lens)))
 
     def run(self, project: Project, rays: Rays | None, ghost: Image) -> Image:

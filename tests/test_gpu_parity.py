@@ -199,6 +199,52 @@ def test_raster_matches_oracle(oracle, key, tile):
     assert np.all(got[..., 3] == 0)
 
 
+def order_key(count: np.ndarray) -> np.ndarray:
+    """rf_tile_order's key: 255 - (leading-one position * 8 + the next three bits), 255 for 0."""
+    c = count.astype(np.int64)
+    e = np.where(c > 0, np.floor(np.log2(np.maximum(c, 1))).astype(np.int64), 0)
+    m = np.where(c > 0, (c << 3 >> e) & 7, 0)
+    return np.where(c > 0, 255 - (e * 8 + m), 255)
+
+
+@pytest.mark.parametrize('tile', [32, 16])
+@pytest.mark.parametrize('key', ['spectral-16-small', 'production-24-small'])
+def test_tile_order_and_ordered_raster(oracle, key, tile):
+    """rf_tile_order is the stable sort of the tiles by decreasing entry count (3 significant
+    bits), and rf_raster_ordered's image equals rf_raster's bit for bit."""
+    w = workload(key)
+    ghost = ghost_texture()
+    spec = light_spectrum()
+    r = oracle_pipeline(oracle, w, ghost, spec)
+    ra = r['raster_args']
+    ra.tile_size = tile
+    vtx_d = dev(r['vtx'])
+    offsets, entries, task = gpu_tiles(ra, dev(r['bounds']), vtx_d)
+    order = task.order(offsets)
+    torch.cuda.synchronize()
+    off = offsets.cpu().numpy().astype(np.int64)
+    tiles = off.size - 1
+    got = order.cpu().numpy()[:tiles].astype(np.int64)
+    want = np.argsort(order_key(np.diff(off)), kind='stable')
+    np.testing.assert_array_equal(got, want)
+    assert len(np.unique(np.diff(off))) > 3  # tiles of different weights
+    ghost_d, spec_d = dev(ghost), dev(spec)
+    images = []
+    for ordered in (False, True):
+        image = torch.empty((ra.height, ra.width, 4), device='cuda')
+        if ordered:
+            st = lib().rf_raster_ordered(vtx_d.data_ptr(), offsets.data_ptr(), entries.data_ptr(), order.data_ptr(),
+                                         ghost_d.data_ptr(), spec_d.data_ptr(), ctypes.byref(ra), image.data_ptr(),
+                                         stream())
+        else:
+            st = lib().rf_raster(vtx_d.data_ptr(), offsets.data_ptr(), entries.data_ptr(), ghost_d.data_ptr(),
+                                 spec_d.data_ptr(), ctypes.byref(ra), image.data_ptr(), stream())
+        check(st, 'raster')
+        images.append(image)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(images[0].cpu().numpy(), images[1].cpu().numpy())
+
+
 @pytest.mark.parametrize('key', ['plain-8', 'production-24-small'])
 def test_raster_skipped_records_add_nothing(oracle, key):
     """The raster leaves out records whose fragments are all zero (a NaN reflectance; or,
