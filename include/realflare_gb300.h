@@ -100,6 +100,39 @@ long long rf_launch_count(void);
 int rf_trace(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
              const rf_trace_args* args, float* rays, void* stream);
 
+/* One surface hit of a traced ray (the reference's Intersection, realflare/api/tasks/
+ * opencl.py:18-25, without the float3 padding): position and unit normal at the surface,
+ * the incidence angle acos(-dir . normal) (0 on flat elements), hit 1 (0 in an unused
+ * record). */
+typedef struct rf_intersection {
+    float pos[3];
+    float normal[3];
+    float incident;
+    int32_t hit;
+} rf_intersection;
+
+/* Replaces IntersectionsTask.raytrace (realflare/api/tasks/raytracing.py:250-348): the
+ * trace kernel built with STORE_INTERSECTIONS (raytracing.cl:229-271). rf_trace into rays,
+ * and every ray's hits into intersections: device rf_intersection[n_rays][intersection_count]
+ * (rays in rf_trace's order), zeroed first; record k of a ray is the hit of its k-th loop
+ * step (aperture and sensor included); steps past intersection_count are not stored. The
+ * reference sizes intersection_count as 3 * element_count - 1. */
+int rf_trace_intersections(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
+                           const rf_trace_args* args, float* rays, rf_intersection* intersections,
+                           int32_t intersection_count, void* stream);
+
+/* Replaces DiagramTask (realflare/api/tasks/diagram.py:24-228) and its kernels lenses and
+ * intersections (realflare/api/tasks/cl/diagram.cl:21-138): the lens cross-section diagram.
+ * image: device float[height][width][4] RGBA, written whole: the optical axis and the
+ * elements' profiles at scale pixels per mm (lenses), then, when intersections is not
+ * NULL, each ray's path between consecutive hits and each hit's normal (intersections).
+ * intersections: device rf_intersection[ray_count][intersection_count], the rays of one
+ * grid column (DiagramTask.update_intersection_slice); a ray's last record is followed by
+ * the next ray's first, and the last ray's by an unused record. */
+int rf_diagram(const rf_lens_element* elements, int32_t element_count, int32_t aperture_index, float scale,
+               const rf_intersection* intersections, int32_t ray_count, int32_t intersection_count,
+               int32_t width, int32_t height, float* image, void* stream);
+
 /* ---- quad setup ------------------------------------------------------------------- */
 /* Replaces the prim_shader kernel (realflare/api/tasks/cl/rasterizing.cl:233-320) and its
  * launch (realflare/api/tasks/rasterizing.py:210-221,321-344). bounds: device float4

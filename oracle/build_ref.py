@@ -5,9 +5,9 @@ cannot run here through OpenCL (no platform). This recipe compiles the kernel so
 **where they lie** in the reference checkout into ``oracle/_ref/librf_ref.so``:
 
 1. each OpenCL program is assembled the way the reference's Python tasks assemble it
-   (``raytracing.py:43-52``, ``rasterizing.py:69-101``, ``starburst.py:22-31``,
-   ``aperture.py:27-36``): host-injected constants and struct declarations, then the
-   ``.cl`` files;
+   (``raytracing.py:43-52,255-265``, ``rasterizing.py:69-101``, ``starburst.py:22-31``,
+   ``aperture.py:27-36``, ``diagram.py:32-43``): host-injected constants and struct
+   declarations, then the ``.cl`` files;
 2. one mechanical rewrite makes OpenCL C parse as C++: vector literals
    ``(floatN)(a, b, ...)`` become ``make_floatN(a, b, ...)``; nothing else is changed;
 3. the result is wrapped in a namespace, followed by ``oracle/ref_harness.inc`` (the
@@ -58,6 +58,13 @@ PROGRAMS = {
         ['noise.cl', 'geometry.cl', 'color.cl', 'starburst.cl'],
     ),
     'aperture': ('', ['noise.cl', 'geometry.cl', 'aperture.cl']),
+    # IntersectionsTask.build (raytracing.py:255-265) and DiagramTask.build (diagram.py:32-43)
+    'raytracing_inter': (
+        _RAY + _LENS + _INTERSECTION + '#define STORE_INTERSECTIONS\n'
+        + 'const int LAMBDA_MIN = 390;\nconst int LAMBDA_MAX = 730;\n',
+        ['raytracing.cl'],
+    ),
+    'diagram': (_RAY + _LENS + _INTERSECTION, ['geometry.cl', 'diagram.cl']),
 }
 
 

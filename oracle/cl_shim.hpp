@@ -120,7 +120,7 @@ struct Swz3 {
     };
 #define RF_VEC3(V, S, V2)                                                  \
     struct alignas(4 * sizeof(S)) V {                                      \
-        union { S s[4]; struct { S x, y, z, w_; }; Swz2<S, V2, 4, 0, 1> xy; Swz3<S, V, 4, 0, 1, 2> xyz; }; \
+        union { S s[4]; struct { S x, y, z, w_; }; Swz2<S, V2, 4, 0, 1> xy; Swz2<S, V2, 4, 2, 1> zy; Swz3<S, V, 4, 0, 1, 2> xyz; }; \
         V() { s[0] = 0; s[1] = 0; s[2] = 0; s[3] = 0; }                    \
         V(S v) { s[0] = v; s[1] = v; s[2] = v; s[3] = 0; }                 \
         V(S a, S b, S c) { s[0] = a; s[1] = b; s[2] = c; s[3] = 0; }       \

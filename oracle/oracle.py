@@ -55,6 +55,8 @@ class Oracle:
             lib.rfo_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
             lib.rfo_aperture_noise_dust.argtypes = [_P, _P, _I, _I, _F, _F]
             lib.rfo_starburst.argtypes = [_P, _P, ctypes.POINTER(StarburstArgs), _P, _I, _I]
+            lib.rfo_trace_intersections.argtypes = [_P, _P, _P, ctypes.POINTER(TraceArgs), _P, _P, _I]
+            lib.rfo_diagram.argtypes = [_P, _I, _I, _F, _P, _I, _I, _I, _I, _P]
             self._libs[variant] = lib
         self.lib = self._libs[variant]
 
@@ -79,6 +81,28 @@ class Oracle:
         self.lib.rfo_trace_d(_ptr(el), _ptr(_c(paths, np.int32)), _ptr(_c(wavelengths, np.float32)),
                              ctypes.byref(args), _ptr(out))
         return out
+
+    def trace_intersections(self, elements, paths, wavelengths, args: TraceArgs, count: int):
+        """(rays [6, n], hits [n, count, 8] float32: pos xyz, normal xyz, incident, hit as int32)."""
+        n = args.path_count * args.wavelength_count * args.grid_count**2
+        rays = np.zeros((6, n), np.float32)
+        inter = np.zeros((n, count, 8), np.float32)
+        self.lib.rfo_trace_intersections(_ptr(_c(elements, elements.dtype)), _ptr(_c(paths, np.int32)),
+                                         _ptr(_c(wavelengths, np.float32)), ctypes.byref(args), _ptr(rays),
+                                         _ptr(inter), count)
+        return rays, inter
+
+    def diagram(self, elements, aperture_index, scale, inter, width, height):
+        """The lens diagram (height, width, 4); inter: [rays, count, 8] records or None."""
+        image = np.zeros((height, width, 4), np.float32)
+        el = _c(elements, elements.dtype)
+        if inter is None:
+            self.lib.rfo_diagram(_ptr(el), len(el), aperture_index, scale, None, 0, 0, width, height, _ptr(image))
+        else:
+            rec = _c(inter, np.float32)
+            self.lib.rfo_diagram(_ptr(el), len(el), aperture_index, scale, _ptr(rec), rec.shape[0], rec.shape[1],
+                                 width, height, _ptr(image))
+        return image
 
     def quad_setup(self, rays, P, W, G, area_orig, min_area):
         Q = (G - 1) ** 2
@@ -170,6 +194,8 @@ class Reference:
             lib.ref_starburst.argtypes = [_P, _I, _I, _P, _I, _F, _F, _F, _P, _F, _P, _P, _I, _I, _I, _I, _P]
             lib.ref_aperture_shape.argtypes = [_P, _I, _I, _F, _F, _I, _F, _F, _F]
             lib.ref_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
+            lib.ref_trace_intersections.argtypes = [_P, _I, _P, _I, _P, _I, _I, _F, _I, _F, _P, _P, _P, _I]
+            lib.ref_diagram.argtypes = [_P, _I, _I, _F, _P, _I, _I, _I, _I, _P]
             Reference._lib = lib
         self.lib = Reference._lib
 
@@ -185,6 +211,29 @@ class Reference:
                            args.wavelength_count, args.aperture_index, args.coating_min_ior, args.grid_count,
                            args.grid_length, _ptr(d), _ptr(out), first, count)
         return out
+
+    def trace_intersections(self, elements, paths, wavelengths_int, args: TraceArgs, count: int):
+        n = args.path_count * args.wavelength_count * args.grid_count**2
+        rays = np.zeros((6, n), np.float32)
+        inter = np.zeros((n, count, 8), np.float32)
+        d = np.array(list(args.direction), np.float32)
+        self.lib.ref_trace_intersections(_ptr(_c(elements, elements.dtype)), args.element_count,
+                                         _ptr(_c(paths, np.int32)), args.path_count,
+                                         _ptr(_c(wavelengths_int, np.int32)), args.wavelength_count,
+                                         args.aperture_index, args.coating_min_ior, args.grid_count,
+                                         args.grid_length, _ptr(d), _ptr(rays), _ptr(inter), count)
+        return rays, inter
+
+    def diagram(self, elements, aperture_index, scale, inter, width, height):
+        image = np.zeros((height, width, 4), np.float32)
+        el = _c(elements, elements.dtype)
+        if inter is None:
+            self.lib.ref_diagram(_ptr(el), len(el), aperture_index, scale, None, 0, 0, width, height, _ptr(image))
+        else:
+            rec = _c(inter, np.float32)
+            self.lib.ref_diagram(_ptr(el), len(el), aperture_index, scale, _ptr(rec), rec.shape[0], rec.shape[1],
+                                 width, height, _ptr(image))
+        return image
 
     def prim_shader(self, rays, P, W, G, area_orig, min_area):
         Q = (G - 1) ** 2

@@ -216,10 +216,12 @@ static void grid_point(int ray_id, int grid_count, real grid_length, real* px, r
 /* raytrace kernel, raytracing.cl:178-359. rays: RF_RAY_PLANES planes of P*W*R floats. */
 /* geom (optional, finite-difference checks): per element radius, center, coating
  * thickness 0 and 1 in double, replacing the element's float fields; dir3 (optional): the
- * light direction in double. */
+ * light direction in double. inter (optional): the ray's hits as built with
+ * STORE_INTERSECTIONS (raytracing.cl:229-271), inter_count records of 8 floats (pos xyz,
+ * normal xyz, incident, hit as int32) per ray, record k = the hit of loop step k. */
 static void trace_one(const rf_lens_element* el, const int32_t* paths, const float* wavelengths,
                       const rf_trace_args* a, size_t idx, float* rays, double* rays_d, size_t n_rays,
-                      const double* geom, const double* dir3) {
+                      const double* geom, const double* dir3, float* inter, int inter_count) {
     const int E = a->element_count;
     const int R = a->grid_count * a->grid_count;
     const int ray_id = (int)(idx % (size_t)R);
@@ -245,11 +247,23 @@ static void trace_one(const rf_lens_element* el, const int32_t* paths, const flo
 
     int step = 0, delta = 1;
     const int disperse = !isnan(el[0].coefficients[0]);
-    int lens_id;
-    for (lens_id = 0; lens_id >= 0 && lens_id < E; lens_id += delta) {
+    int lens_id, inter_id = 0;
+    for (lens_id = 0; lens_id >= 0 && lens_id < E; lens_id += delta, inter_id++) {
         const rf_lens_element* e = &el[lens_id];
         hit_t h = intersect_rc(pos, dir, RFO_RADIUS(lens_id), RFO_CENTER(lens_id));
         if (!h.hit) break;
+        if (inter && inter_id < inter_count) {
+            float* o = inter + (idx * (size_t)inter_count + (size_t)inter_id) * 8;
+            const int32_t one = 1;
+            o[0] = (float)h.pos.x;
+            o[1] = (float)h.pos.y;
+            o[2] = (float)h.pos.z;
+            o[3] = (float)h.normal.x;
+            o[4] = (float)h.normal.y;
+            o[5] = (float)h.normal.z;
+            o[6] = (float)h.incident;
+            memcpy(o + 7, &one, sizeof one);
+        }
         pos = h.pos;
         if (lens_id == a->aperture_index) {
             apt_x = h.pos.x / (real)e->height;
@@ -319,7 +333,7 @@ int rfo_trace(const rf_lens_element* el, const int32_t* paths, const float* wave
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL);
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL, NULL, 0);
     return 0;
 }
 
@@ -330,7 +344,7 @@ int rfo_trace_geom_d(const rf_lens_element* el, const int32_t* paths, const floa
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, geom, dir3);
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, geom, dir3, NULL, 0);
     return 0;
 }
 
@@ -340,7 +354,21 @@ int rfo_trace_d(const rf_lens_element* el, const int32_t* paths, const float* wa
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, NULL, NULL);
+    for (long long i = 0; i < (long long)n; i++) trace_one(el, paths, wavelengths, a, (size_t)i, NULL, rays, n, NULL, NULL, NULL, 0);
+    return 0;
+}
+
+/* rfo_trace that also stores every ray's hits (IntersectionsTask.raytrace,
+ * raytracing.py:250-348): inter = n_rays * inter_count records of 8 floats, zeroed first
+ * (update_intersections allocates zeros, raytracing.py:115-123). */
+int rfo_trace_intersections(const rf_lens_element* el, const int32_t* paths, const float* wavelengths,
+                            const rf_trace_args* a, float* rays, float* inter, int inter_count) {
+    const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
+    const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
+    memset(inter, 0, sizeof(float) * 8 * n * (size_t)inter_count);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < (long long)n; i++)
+        trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL, inter, inter_count);
     return 0;
 }
 
@@ -350,7 +378,7 @@ int rfo_trace_range(const rf_lens_element* el, const int32_t* paths, const float
     const size_t R = (size_t)a->grid_count * (size_t)a->grid_count;
     const size_t n = (size_t)a->path_count * (size_t)a->wavelength_count * R;
 #pragma omp parallel for schedule(dynamic, 4096)
-    for (long long i = first; i < first + count; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL);
+    for (long long i = first; i < first + count; i++) trace_one(el, paths, wavelengths, a, (size_t)i, rays, NULL, n, NULL, NULL, NULL, 0);
     return 0;
 }
 
@@ -1014,6 +1042,74 @@ int rfo_starburst(const float* spectrum, const float* light_spectrum, const rf_s
             for (int c = 0; c < 4; c++) acc[c] *= (real)a->intensity;
             float* out = image + 4 * ((size_t)y * w + x);
             xyz_to_ap1(acc, out);
+        }
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------- lens diagram
+ * DiagramTask (realflare/api/tasks/diagram.py:24-228): the kernels lenses
+ * (realflare/api/tasks/cl/diagram.cl:21-67) and intersections (70-138) in FP32, one after
+ * the other per pixel. pow(v, 2) is taken as v * v. inter: rays * count records of 8 floats
+ * (rfo_trace_intersections); the record after the last one reads as unused. */
+static int diagram_is_line(float posx, float posy, float p0x, float p0y, float p1x, float p1y, float width) {
+    float vx = p1x - p0x, vy = p1y - p0y;
+    float ax = posx - p0x, ay = posy - p0y;
+    float bx = posx - p1x, by = posy - p1y;
+    int between = (vx * ax + vy * ay) > 0.0f && (vx * bx + vy * by) < 0.0f;
+    float d = fabsf(vx * ay - ax * vy) / sqrtf(vx * vx + vy * vy);
+    return between && d <= width / 2.0f;
+}
+
+static int diagram_hit(const float* inter, long long i, long long total) {
+    int32_t h = 0;
+    if (i < total) memcpy(&h, inter + 8 * i + 7, sizeof h);
+    return h != 0;
+}
+
+int rfo_diagram(const rf_lens_element* el, int E, int aperture, float scale, const float* inter, int rays,
+                int count, int width, int height, float* image) {
+    const long long total = inter ? (long long)rays * count : 0;
+#pragma omp parallel for schedule(static)
+    for (int py = 0; py < height; py++) {
+        for (int px = 0; px < width; px++) {
+            float x = (float)px, y = (float)(height / 2 - py);
+            float rgba[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if ((int)y == 0) rgba[0] = 1.0f;
+            for (int i = 0; i < E; i++) {
+                float r = el[i].radius * scale, h = el[i].height * scale, c = el[i].center * scale;
+                if (r == 0.0f && fabsf(y) < h && (int)x == (int)c) {
+                    if (i == aperture || i == E - 1) rgba[1] = 1.0f;
+                    else rgba[2] = 1.0f;
+                    break;
+                }
+                float ex = x - c;
+                float r_circle = sqrtf(ex * ex + y * y);
+                int draw_half = (r > 0.0f) ? (x < c) : (x > c);
+                if (draw_half && (int)fabsf(r) == (int)r_circle && fabsf(y) < h) rgba[2] = 1.0f;
+            }
+            for (int ray = 0; inter && ray < rays; ray++) {
+                for (int k = 0; k < count; k++) {
+                    long long i1 = (long long)ray * count + k;
+                    if (!diagram_hit(inter, i1 + 1, total)) break;
+                    const float* s = inter + 8 * i1;
+                    const float* t = s + 8;
+                    float p0x = (s[2] * scale) * -1.0f, p0y = (s[1] * scale) * -1.0f;
+                    float p1x = (t[2] * scale) * -1.0f, p1y = (t[1] * scale) * -1.0f;
+                    float nx = s[5] * scale, ny = s[4] * scale;
+                    if (diagram_is_line(x, y, p0x, p0y, p0x - nx * 1.0f, p0y - ny * 1.0f, 1.0f)) {
+                        rgba[0] = 0.25f;
+                        rgba[1] = rgba[2] = rgba[3] = 0.0f;
+                    }
+                    if (p1x == 0.0f) break;
+                    if (diagram_is_line(x, y, p0x, p0y, p1x, p1y, 1.0f)) {
+                        rgba[0] += 0.25f;
+                        rgba[1] += 0.25f;
+                        rgba[2] += 0.25f;
+                    }
+                }
+            }
+            memcpy(image + 4 * ((size_t)py * width + px), rgba, sizeof rgba);
         }
     }
     return 0;

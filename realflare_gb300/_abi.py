@@ -145,6 +145,8 @@ F32 = ctypes.c_float
 # name -> argtypes (every entry point returns int status)
 SIGNATURES = {
     'rf_trace': [P, P, P, ctypes.POINTER(TraceArgs), P, P],
+    'rf_trace_intersections': [P, P, P, ctypes.POINTER(TraceArgs), P, P, I32, P],
+    'rf_diagram': [P, I32, I32, F32, P, I32, I32, I32, I32, P, P],
     'rf_quad_setup': [P, I32, I32, I32, F32, F32, P, P, P],
     'rf_vertex': [P, P, I32, I32, I32, F32, I32, I32, P, P],
     'rf_bin_masks': [P, I32, F32, I32, I32, I32, P, P],

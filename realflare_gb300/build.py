@@ -37,6 +37,7 @@ UNITS = {
     'rf_batch.cu': [],
     # the adjoint re-traces rays: it must use the trace's arithmetic
     'rf_adjoint.cu': ['-ftz=true'] + ([] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false']),
+    'rf_diagram.cu': ['-ftz=true'] + ([] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false']),
 }
 
 

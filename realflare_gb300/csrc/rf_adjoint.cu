@@ -133,6 +133,7 @@ struct StepRecorder {
         if (n < kAdjMaxSteps) steps[n] = {px, py, pz, dx, dy, dz, lens};
         n++;
     }
+    __device__ __forceinline__ void hit(int, const Hit&, float, float, float, bool) {}
     __device__ __forceinline__ void rrel(float r, float) {
         if (r > best) {
             best = r;

@@ -168,11 +168,14 @@ struct TraceFrame {
     float dir[3];  // normalize(-direction.xyz), host-computed in FP32
 };
 
-// Observer of a traced ray for the adjoint: step() sees the ray entering each element
-// (element index, position, direction), rrel() each candidate of the running maximum before
-// it is taken, reflect() each reflection. The forward trace uses NoRecord (inlined away).
+// Observer of a traced ray: step() sees the ray entering each element (element index,
+// position, direction), hit() each successful intersection (loop step index, the hit, the
+// incoming direction, whether the element is flat), rrel() each candidate of the running
+// maximum before it is taken, reflect() each reflection. The adjoint records steps, the
+// intersection trace records hits; the forward trace uses NoRecord (inlined away).
 struct NoRecord {
     __device__ __forceinline__ void step(int, float, float, float, float, float, float) {}
+    __device__ __forceinline__ void hit(int, const Hit&, float, float, float, bool) {}
     __device__ __forceinline__ void rrel(float, float) {}
     __device__ __forceinline__ void reflect() {}
 };
@@ -207,12 +210,13 @@ __device__ __forceinline__ void trace_ray_rec(const SmemElement* __restrict__ se
     float apt_x = 0.0f, apt_y = 0.0f, rrel = 0.0f, refl = 1.0f;
 
     int step = 0, delta = 1;
-    int lens_id;
-    for (lens_id = 0; lens_id >= 0 && lens_id < E; lens_id += delta) {
+    int lens_id, inter_id = 0;  // inter_id: loop steps so far (raytracing.cl:256)
+    for (lens_id = 0; lens_id >= 0 && lens_id < E; lens_id += delta, inter_id++) {
         const SmemElement& e = se[lens_id];
         rec.step(lens_id, px, py, pz, dx, dy, dz);
         Hit h = intersect(px, py, pz, dx, dy, dz, e);
         if (!h.hit) break;
+        rec.hit(inter_id, h, dx, dy, dz, e.radius == 0.0f);
         px = h.px;
         py = h.py;
         pz = h.pz;

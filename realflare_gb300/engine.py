@@ -48,7 +48,10 @@ class Engine:
             RenderElement.GHOST: self.ghost,
             RenderElement.FLARE: self.flare,
             RenderElement.FLARE_STARBURST: self.flare_starburst,
+            RenderElement.DIAGRAM: self.diagram,
         }
+        self.intersection_task = tasks.IntersectionsTask(self.queue)
+        self.diagram_task = tasks.DiagramTask(self.queue)
         self._initialized = True
 
     def starburst_aperture(self, project: Project) -> Image:
@@ -136,6 +139,12 @@ class Engine:
         check(tasks.lib().rf_axpby(ptr(ft), 2.0, ptr(st), 1.0, ptr(out), ft.numel(),
                                    self.rasterizing_task.stream), 'rf_axpby')
         return Image(tensor=out, args=(flare.args, starburst.args))
+
+    def diagram(self, project: Project) -> Image:
+        # engine.py:189-193: the debug ghost's rays over the lens cross-section
+        path_indexes = (project.diagram.debug_ghost,)
+        intersections = self.intersection_task.run(project, path_indexes)
+        return self.diagram_task.run(project, intersections)
 
     def render(self, project: Project) -> bool:
         if not self._initialized:

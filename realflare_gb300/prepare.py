@@ -7,13 +7,14 @@ quad area, bin sizes and scale factors for the raster.
 """
 from __future__ import annotations
 
+import copy
 from dataclasses import dataclass
 
 import numpy as np
 
 from . import lens as lens_mod
 from ._abi import RasterArgs, TraceArgs
-from .data import Project, RealflareError
+from .data import Project, QPointF, QSize, RealflareError
 
 
 @dataclass
@@ -99,3 +100,35 @@ def quad_constants(project: Project) -> tuple:
     """(area_orig, rel_min_area) of ``rasterizing.py:328-329``."""
     area = lens_mod.area_orig(project.render.grid_count, project.render.grid_length)
     return area, project.flare.lens.min_area * area
+
+
+def diagram_project(project: Project) -> Project:
+    """The project IntersectionsTask traces (``raytracing.py:362-380``): light at
+    (0, diagram.light_position), the diagram's grid, grid length and resolution (which sets
+    the light direction's aspect), one wavelength."""
+    p = copy.deepcopy(project)
+    d = project.diagram
+    p.flare.light.position = QPointF(0.0, float(d.light_position))
+    p.render.grid_count = d.grid_count
+    p.render.grid_length = d.grid_length
+    p.render.resolution = QSize(d.resolution.width(), d.resolution.height())
+    p.render.wavelength_count = 1
+    p.render.wavelengths = ()
+    return p
+
+
+def intersection_count(element_count: int) -> int:
+    """Hit records per ray (``raytracing.py:326``): three per element, less one."""
+    return element_count * 3 - 1
+
+
+def diagram_scale(project: Project) -> float:
+    """Pixels per mm of the diagram (``diagram.py:45-57``): the image width less 10 pixels of
+    padding over the lens model's total element distance (1 when that is 0)."""
+    model = lens_mod.resolve_model(project.flare.lens)
+    distance = 0.0
+    for e in model.lens_elements:
+        distance += e.distance
+    if distance == 0:
+        return 1.0
+    return (project.diagram.resolution.width() - 10) / distance

@@ -32,7 +32,7 @@ from .._abi import (
 )
 from ..constants import LAMBDA_MID, light_spectrum
 from ..data import Project, QPointF, QSize, RealflareError
-from ..device import Image, Rays, empty, ptr, require_cuda, stream_handle, to_device
+from ..device import Image, MemoryObject, Rays, empty, ptr, require_cuda, stream_handle, to_device
 
 
 class Task:
@@ -80,6 +80,66 @@ class RaytracingTask(Task):
 
     def run(self, project: Project, path_indexes: tuple = (), paths=None) -> Rays | None:
         return self.raytrace(project, path_indexes, paths)
+
+
+class IntersectionsTask(Task):
+    """The trace with every surface hit stored, for the lens diagram
+    (``realflare/api/tasks/raytracing.py:250-380``): the diagram's light position, grid and
+    resolution, one wavelength. ``run`` returns a ``MemoryObject`` whose tensor is float32
+    [paths, 1, grid, grid, 3 * elements - 1, 8] (rf_intersection records: pos xyz, normal
+    xyz, incident, hit as int32), or None without a lens or without paths."""
+
+    def run(self, project: Project, path_indexes: tuple) -> MemoryObject | None:
+        p = prepare.diagram_project(project)
+        inputs = prepare.trace_inputs(p, path_indexes=path_indexes)
+        if inputs is None or inputs.ray_count == 0:
+            return None
+        a = inputs.args
+        count = prepare.intersection_count(a.element_count)
+        elements = to_device(inputs.elements.view(np.uint8))
+        paths_t = to_device(inputs.paths)
+        wl = to_device(inputs.wavelengths)
+        rays = empty((6, inputs.ray_count))
+        inter = empty((inputs.ray_count, count, 8))
+        check(self.lib.rf_trace_intersections(ptr(elements), ptr(paths_t), ptr(wl), ctypes.byref(a), ptr(rays),
+                                              ptr(inter), count, self.stream), 'rf_trace_intersections')
+        G = a.grid_count
+        result = MemoryObject(tensor=inter.view(a.path_count, a.wavelength_count, G, G, count, 8),
+                              args=(bytes(a), inputs.paths.tobytes()))
+        result.rays = rays
+        return result
+
+
+class DiagramTask(Task):
+    """The lens cross-section with the traced rays (``realflare/api/tasks/diagram.py:24-228``):
+    rf_diagram draws the optical axis and element profiles, then the paths and normals of
+    one grid column of rays (column (grid - 1) // 2 + diagram.column_offset, sliced as the
+    reference slices its array)."""
+
+    def run(self, project: Project, intersections: MemoryObject | None) -> Image:
+        r = project.diagram.resolution
+        w, h = r.width(), r.height()
+        image = empty((h, w, 4))
+        inputs = prepare.trace_inputs(prepare.diagram_project(project), paths=np.zeros((0, 2), np.int32))
+        if inputs is None:  # no lens: the reference's lenses kernel does not run
+            image.zero_()
+            return Image(tensor=image, args=(hash(project.diagram), None))
+        elements = to_device(inputs.elements.view(np.uint8))
+        scale = np.float32(prepare.diagram_scale(project))
+        records, rays, count = None, 0, 0
+        if intersections is not None:
+            t = intersections.tensor
+            column = int((t.shape[3] - 1) / 2) + project.diagram.column_offset
+            part = t[:, :, :, column:column + 1].contiguous()  # DiagramTask.update_intersection_slice
+            rays, count = part.shape[2] * part.shape[3], part.shape[4]
+            if rays > 0 and part.shape[0] > 0:
+                records = part[0, 0].reshape(rays, count, 8).contiguous()
+            else:
+                rays = 0
+        check(self.lib.rf_diagram(ptr(elements), inputs.args.element_count, inputs.args.aperture_index, float(scale),
+                                  ptr(records) if records is not None else None, rays, count, w, h, ptr(image),
+                                  self.stream), 'rf_diagram')
+        return Image(tensor=image, args=(hash(project.diagram), intersections.args if intersections else None))
 
 
 class RasterizingTask(Task):

@@ -82,3 +82,48 @@ def test_aperture_and_starburst_match_reference_kernels(pair):
     a.offset[0], a.offset[1] = 0.2, -0.1
     a.scale[0], a.scale[1] = 1.0, 1.2
     assert np.array_equal(o.starburst(spec, light_spectrum(), a), r.starburst(spec, light_spectrum(), a))
+
+
+def diagram_case(o_or_r, w, diagram_width=384, diagram_height=192):
+    """The diagram's trace of a reduced workload (three ghost paths, the diagram's settings)
+    and the slice of the centre grid column."""
+    from realflare_gb300.data import QSize
+
+    p = w.project
+    p.diagram.resolution = QSize(diagram_width, diagram_height)
+    p.diagram.grid_count = 9
+    p.diagram.grid_length = 30.0
+    p.diagram.light_position = 0.3
+    dp = prepare.diagram_project(p)
+    ti = prepare.trace_inputs(dp, paths=w.paths[:3])
+    count = prepare.intersection_count(ti.args.element_count)
+    return p, ti, count
+
+
+@pytest.mark.parametrize('name', ['plain-8', 'spectral-16'])
+def test_intersections_and_diagram_match_reference_kernels(pair, name):
+    """IntersectionsTask's trace (STORE_INTERSECTIONS) and DiagramTask's two kernels: the
+    oracle's records and diagram images equal the reference kernels' (integer wavelengths)."""
+    o, r = pair
+    w = reduced(name)
+    w.project.flare.lens.coating_thickness = ()
+    p, ti, count = diagram_case(o, w)
+    a = ti.args
+    rays_o, inter_o = o.trace_intersections(ti.elements, ti.paths, ti.wavelengths, a, count)
+    rays_r, inter_r = r.trace_intersections(ti.elements, ti.paths, ti.wavelengths.astype(np.int32), a, count)
+    assert nan_equal(rays_o, rays_r)
+    assert np.array_equal(inter_o.view(np.int32), inter_r.view(np.int32))
+    hits = inter_r[..., 7].view(np.int32)
+    assert hits.sum() > a.element_count * 4  # rays do cross the lens
+    G = a.grid_count
+    column = (G - 1) // 2
+    part = inter_r.reshape(a.path_count, 1, G, G, count, 8)[0, 0, :, column]
+    scale = np.float32(prepare.diagram_scale(p))
+    res = p.diagram.resolution
+    for rec in (None, part):
+        img_o = o.diagram(ti.elements, a.aperture_index, scale, rec, res.width(), res.height())
+        img_r = r.diagram(ti.elements, a.aperture_index, scale, rec, res.width(), res.height())
+        assert np.array_equal(img_o, img_r)
+        assert (img_r[..., 2] > 0).sum() > 100  # element profiles
+        if rec is not None:
+            assert (img_r[..., 0] == 0.25).sum() > 100  # ray segments
