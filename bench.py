@@ -53,6 +53,8 @@ def parse_args():
                     help='frames of the batched form measured beside the plain path (0 = skip)')
     ap.add_argument('--no-differentiable', action='store_true',
                     help='skip the forward+adjoint measurement of the 16-surface lens')
+    ap.add_argument('--no-diagram', action='store_true',
+                    help='skip the DIAGRAM element measurement (trace with hits and drawing)')
     ap.add_argument('--raster-stats', action='store_true',
                     help='count k_raster work (statistics build of the library) instead of timing')
     return ap.parse_args()
@@ -536,6 +538,7 @@ def main() -> None:
         e2e = run_e2e(w, args)
     batched = run_batched(args) if args.batched_frames > 0 and rank == 0 else None
     differentiable = run_differentiable(args) if not args.no_differentiable and rank == 0 else None
+    diagram = run_diagram(args) if not args.no_diagram and rank == 0 else None
 
     peak, peak_kind = load_peaks()
     raster_s = last['raster'] / 1e3
@@ -586,6 +589,7 @@ def main() -> None:
             'gpu_launches': launches,
             'batched': batched,
             'differentiable': differentiable,
+            'diagram': diagram,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -757,6 +761,63 @@ def run_differentiable(args) -> dict:
                      'param_rms_error_start': rec.error_start, 'param_rms_error_end': rec.error_end,
                      'seconds': rec.seconds},
         'timing': 'wall clock per iteration (each includes the binning host synchronisation)',
+    }
+
+
+def run_diagram(args) -> dict:
+    """The DIAGRAM element at the reference's default diagram settings (2048 x 1024, 8 x 8
+    grid, grid length 50, one ghost) on the workload's lens: GPU milliseconds per render (the
+    trace with every hit stored, then the drawing; CUDA events on the tasks' stream, inputs
+    uploaded each render), and the reference's own kernels (oracle/_ref, else the C
+    oracle) on the same inputs on the host cores."""
+    import numpy as np
+    import torch
+
+    from oracle import oracle as orc
+    from realflare_gb300 import prepare, synthetic
+    from realflare_gb300.tasks import DiagramTask, IntersectionsTask
+
+    p = synthetic.workload(args.workload).project
+    d = p.diagram
+    stream = torch.cuda.Stream()
+    inter_task, draw_task = IntersectionsTask(stream), DiagramTask(stream)
+
+    def render():
+        with torch.cuda.stream(stream):
+            return draw_task.run(p, inter_task.run(p, (d.debug_ghost,)))
+
+    for _ in range(3):
+        image = render()
+    n = 20
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    start.record(stream)
+    for _ in range(n):
+        render()
+    end.record(stream)
+    end.synchronize()
+    gpu_ms = start.elapsed_time(end) / n
+    got = image.tensor.cpu().numpy()
+
+    ti = prepare.trace_inputs(prepare.diagram_project(p), path_indexes=(d.debug_ghost,))
+    a = ti.args
+    count = prepare.intersection_count(a.element_count)
+    G = a.grid_count
+    scale = np.float32(prepare.diagram_scale(p))
+    try:
+        cpu, kind, wl = orc.Reference(), 'reference', ti.wavelengths.astype(np.int32)
+    except (OSError, RuntimeError):
+        cpu, kind, wl = orc.Oracle('f32'), 'port', ti.wavelengths
+    t0 = time.perf_counter()
+    _, inter = cpu.trace_intersections(ti.elements, ti.paths, wl, a, count)
+    part = inter.reshape(a.path_count, 1, G, G, count, 8)[:, :, :, (G - 1) // 2 + d.column_offset]
+    want = cpu.diagram(ti.elements, a.aperture_index, scale, part[0, 0] if part.size else None,
+                       d.resolution.width(), d.resolution.height())
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    return {
+        'element': 'DIAGRAM', 'image': f'{d.resolution.width()}x{d.resolution.height()}', 'grid': G,
+        'ghost_paths': a.path_count, 'gpu_ms': gpu_ms, 'cpu_ms': cpu_ms, 'cpu_kind': kind,
+        'cpu_cores': os.cpu_count(), 'equal_to_cpu': bool(np.array_equal(got, want)),
     }
 
 
