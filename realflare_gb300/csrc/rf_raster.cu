@@ -69,7 +69,7 @@ struct alignas(16) Rec {
     int bb[4];       // xmin, xmax, ymin, ymax
     float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad
     float qf[8];     // q as floats (exact: |q| < 2^24)
-    float uv[8];     // ghost texture coordinates (u0, v0, ..., u3, v3)
+    float uv[8];     // ghost texel coordinates of the corners (u0, v0, ..., u3, v3), see store_corner
     float rrel[4], inten[4], refl[4];
     int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
     int flags;       // 1: bounds rejection is exact; 2: adds nothing (collinear, or zero_record)
@@ -245,7 +245,10 @@ __device__ __forceinline__ float ghost_sample(const float* __restrict__ tex, int
         t01 = (i0_in && j1_in) ? __ldg(row1 + ia) : 0.0f;
         t11 = (i1_in && j1_in) ? __ldg(row1 + ib) : 0.0f;
     }
-    return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
+    // the specification's (1-a)(1-b) t00 + a(1-b) t10 + (1-a) b t01 + a b t11, as three
+    // interpolations (the same value up to rounding)
+    const float top = fmaf(a, t10 - t00, t00), bottom = fmaf(a, t11 - t01, t01);
+    return fmaf(b, bottom - top, top);
 }
 
 // fragment_shader (rasterizing.cl:471-506) times the hit count. The texture coordinate
@@ -258,7 +261,7 @@ __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], c
     const float4 uv01 = ld4(r.uv), uv23 = ld4(r.uv + 4);
     const float u = w[0] * uv01.x + w[1] * uv01.z + w[2] * uv23.x + w[3] * uv23.z;
     const float v = w[0] * uv01.y + w[1] * uv01.w + w[2] * uv23.y + w[3] * uv23.w;
-    const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox, v * fc.tsy + fc.toy);
+    const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u, v);
     const float4 rl = ld4(r.rrel);
     const float rr = w[0] * rl.x + w[1] * rl.y + w[2] * rl.z + w[3] * rl.w;
     // smoothstep(1, 0.95, rr) with the division by the constant (0.95 - 1) as a product
@@ -302,11 +305,14 @@ __device__ __forceinline__ void load_corner(const float4* __restrict__ vtx, uint
     c.b0 = __ldg(vtx + 2 * vi + 2);
     c.b1 = __ldg(vtx + 2 * vi + 3);
 }
-// mix_vertex (rasterizing.cl:509-522) of one corner into record r
-__device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t, int S, Rec& r) {
+// mix_vertex (rasterizing.cl:509-522) of one corner into record r. The texture coordinate
+// is stored in texels, uv * tex_scale + tex_offset (fragment_fast): the weights sum to one,
+// so interpolating texel coordinates is the fragment's ((uv / scale + 1) / 2) * size - 0.5.
+__device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t, int S, const FragmentConsts& fc,
+                                             Rec& r) {
     const float px = c.a0.x + (c.b0.x - c.a0.x) * t, py = c.a0.y + (c.b0.y - c.a0.y) * t;
-    r.uv[2 * k] = c.a0.z + (c.b0.z - c.a0.z) * t;
-    r.uv[2 * k + 1] = c.a0.w + (c.b0.w - c.a0.w) * t;
+    r.uv[2 * k] = (c.a0.z + (c.b0.z - c.a0.z) * t) * fc.tsx + fc.tox;
+    r.uv[2 * k + 1] = (c.a0.w + (c.b0.w - c.a0.w) * t) * fc.tsy + fc.toy;
     r.rrel[k] = c.a1.x + (c.b1.x - c.a1.x) * t;
     r.refl[k] = c.a1.y + (c.b1.y - c.a1.y) * t;
     r.inten[k] = c.a1.z + (c.b1.z - c.a1.z) * t;
@@ -467,7 +473,8 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
         for (int h = 0; h < kLoads; h++) {
             const int e = my_entry + 64 * h;
             if (have_next[h])
-                for (int i = 0; i < p.WS; i++) store_corner(next[h], my_corner, blend[i], S, dst[e * p.WS + i]);
+                for (int i = 0; i < p.WS; i++)
+                    store_corner(next[h], my_corner, blend[i], S, fc, dst[e * p.WS + i]);
         }
         __syncwarp();  // the four corners of each record are stored
 #pragma unroll
@@ -546,10 +553,8 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                     if (!in_image) continue;
                     int hits = S;
                     if (!is_whole) {
-                        if (r.flags & 1) {
-                            const int4 bb = *reinterpret_cast<const int4*>(r.bb);
-                            if (sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w) continue;
-                        }
+                        // (a bounds test first would save nothing: the block was selected
+                        // because the bounds touch it, so some lane tests coverage anyway)
                         hits = 0;
                         for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
                         if (hits == 0) continue;
@@ -768,7 +773,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
             if (e < per_batch && base + e < end) {
                 CornerLoad c;
                 load_corner(vtx, tile_entries[base + e], my_corner, p, c);
-                for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, recs[e * p.WS + i]);
+                for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, fc, recs[e * p.WS + i]);
             }
         }
         __syncthreads();
@@ -827,14 +832,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         if ((whole[m] >> b) & 1u) {
                             hits = S;
                         } else {
-                            bool test = true;
-                            if (r.flags & 1) {
-                                const int4 bb = *reinterpret_cast<const int4*>(r.bb);
-                                test = !(sx0 + S - 1 < bb.x || sx0 > bb.y || sy0 + S - 1 < bb.z || sy0 > bb.w);
-                            }
-                            if (test)
-                                for (int s = 0; s < S; s++)
-                                    hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
+                            for (int s = 0; s < S; s++) hits += inside(r, sx0 + s, sy0 + SUB_OFFSETS[S - 1 + s]) ? 1 : 0;
                         }
                     }
                     if (!__any_sync(0xffffffffu, hits > 0)) continue;
@@ -853,8 +851,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         const float u = wt[0] * uv01.x + wt[1] * uv01.z + wt[2] * uv23.x + wt[3] * uv23.z;
                         const float v = wt[0] * uv01.y + wt[1] * uv01.w + wt[2] * uv23.y + wt[3] * uv23.w;
                         float dgu, dgv;
-                        const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u * fc.tsx + fc.tox,
-                                                           v * fc.tsy + fc.toy, dgu, dgv);
+                        const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u, v, dgu, dgv);
                         const float4 rl = ld4(r.rrel);
                         const float rr = wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w;
                         const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
@@ -952,8 +949,8 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
                         const long long vi = (path * VC + corners[c]) * p.W + w;
                         const float4 a0 = vtx[2 * vi], a1 = vtx[2 * vi + 1], b0 = vtx[2 * vi + 2], b1 = vtx[2 * vi + 3];
                         const float px = a0.x + (b0.x - a0.x) * sub_pos, py = a0.y + (b0.y - a0.y) * sub_pos;
-                        r.uv[2 * c] = a0.z + (b0.z - a0.z) * sub_pos;
-                        r.uv[2 * c + 1] = a0.w + (b0.w - a0.w) * sub_pos;
+                        r.uv[2 * c] = (a0.z + (b0.z - a0.z) * sub_pos) * fc.tsx + fc.tox;
+                        r.uv[2 * c + 1] = (a0.w + (b0.w - a0.w) * sub_pos) * fc.tsy + fc.toy;
                         r.rrel[c] = a1.x + (b1.x - a1.x) * sub_pos;
                         r.refl[c] = a1.y + (b1.y - a1.y) * sub_pos;
                         r.inten[c] = a1.z + (b1.z - a1.z) * sub_pos;
