@@ -8,6 +8,7 @@ from __future__ import annotations
 import json
 import math
 import os
+from functools import lru_cache
 
 import numpy as np
 
@@ -35,6 +36,21 @@ def resolve_model(lens) -> LensModel:
     return model_from_path(os.path.expandvars(lens.lens_model_path))
 
 
+@lru_cache(16)
+def _catalogue(glasses_path: str) -> tuple:
+    """The glasses of a catalogue directory, read once per path (the reference caches its
+    lens elements per glasses path the same way, ``raytracing.py:54-73``)."""
+    return tuple(glass.glasses_from_path(glasses_path))
+
+
+@lru_cache(4096)
+def _closest_coefficients(glasses_path: str, n: float, v: float, v_offset: float):
+    """Sellmeier coefficients of the closest catalogue glass, or None; keyed by the
+    catalogue's path rather than its glasses, which are costly to hash."""
+    closest = glass.closest_glass(_catalogue(glasses_path), n, v, v_offset)
+    return tuple(closest.coefficients[:6]) if closest else None
+
+
 def elements(
     lens_model: LensModel,
     sensor_size: tuple,
@@ -54,7 +70,7 @@ def elements(
     lens_elements = list(lens_model.lens_elements)
     sensor_length = float(np.linalg.norm(sensor_size) / 2)
     lens_elements.append(LensElement(height=sensor_length))
-    glasses = tuple(glass.glasses_from_path(glasses_path))
+    glasses = _catalogue(glasses_path)
 
     array = np.zeros(len(lens_elements), lens_element_dtype)
     if not glasses:
@@ -75,11 +91,10 @@ def elements(
             else:
                 array[i]['coating_layers'] = 2
                 array[i]['coating_thickness'][:] = t[:2]
-        closest = glass.closest_glass(
-            glasses, element.refractive_index, element.abbe_nr, abbe_nr_adjustment
-        )
-        if closest:
-            array[i]['coefficients'][:6] = closest.coefficients[:6]
+        coefficients = _closest_coefficients(glasses_path, element.refractive_index, element.abbe_nr,
+                                             abbe_nr_adjustment)
+        if coefficients:
+            array[i]['coefficients'][:6] = coefficients
         offset += element.distance
     return array
 
