@@ -70,14 +70,15 @@ struct alignas(16) Rec {
     float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad
     float qf[8];     // q as floats (exact: |q| < 2^24)
     float uv[8];     // ghost texel coordinates of the corners (u0, v0, ..., u3, v3), see store_corner
-    float rrel[4], inten[4], refl[4];
+    float rs[4];     // (rrel - 1) / (0.95 - 1): smoothstep(1, 0.95, rrel)'s ramp before clamping
+    float inten[4], refl[4];
     int ec[15];      // edges 01, 12, 23, 30, 20: l = A * y + B * x + C (bias folded into C)
     int flags;       // 1: bounds rejection is exact; 2: adds nothing (collinear, or zero_record)
     int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
     int color;       // w * WS + i
 };
 static_assert(sizeof(Rec) == 256 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0 &&
-                  offsetof(Rec, qf) % 16 == 0 && offsetof(Rec, uv) % 16 == 0 && offsetof(Rec, rrel) % 16 == 0 &&
+                  offsetof(Rec, qf) % 16 == 0 && offsetof(Rec, uv) % 16 == 0 && offsetof(Rec, rs) % 16 == 0 &&
                   offsetof(Rec, inten) % 16 == 0 && offsetof(Rec, refl) % 16 == 0 &&
                   offsetof(Rec, ec) % 16 == 0 && offsetof(Rec, flags) == offsetof(Rec, ec) + 15 * sizeof(int),
               "records are read with 16-byte loads");
@@ -262,10 +263,10 @@ __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], c
     const float u = w[0] * uv01.x + w[1] * uv01.z + w[2] * uv23.x + w[3] * uv23.z;
     const float v = w[0] * uv01.y + w[1] * uv01.w + w[2] * uv23.y + w[3] * uv23.w;
     const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u, v);
-    const float4 rl = ld4(r.rrel);
-    const float rr = w[0] * rl.x + w[1] * rl.y + w[2] * rl.z + w[3] * rl.w;
-    // smoothstep(1, 0.95, rr) with the division by the constant (0.95 - 1) as a product
-    const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
+    // smoothstep(1, 0.95, rrel): the ramp (rrel - 1) / (0.95 - 1) is linear in rrel, so the
+    // corners' ramps interpolate to the fragment's (the weights sum to one)
+    const float4 rl = ld4(r.rs);
+    const float st = __saturatef(w[0] * rl.x + w[1] * rl.y + w[2] * rl.z + w[3] * rl.w);
     const float ri = st * st * (3.0f - 2.0f * st);
     const float4 in = ld4(r.inten), rf = ld4(r.refl);
     float ai = w[0] * in.x + w[1] * in.y + w[2] * in.z + w[3] * in.w;
@@ -284,6 +285,9 @@ __host__ __device__ inline FragmentConsts fragment_consts(const RasterParams& p)
     fc.toy = (float)(0.5 * p.ghost_h - 0.5);
     return fc;
 }
+
+// 1 / (0.95 - 1), the smoothstep ramp's slope (fragment_shader, rasterizing.cl:487-488)
+constexpr float kRampScale = 1.0f / (0.95f - 1.0f);
 
 // Corner k of entry `entry` at the pair's two wavelengths: vertex words a0, a1 (first
 // wavelength) and b0, b1 (second).
@@ -313,7 +317,7 @@ __device__ __forceinline__ void store_corner(const CornerLoad& c, int k, float t
     const float px = c.a0.x + (c.b0.x - c.a0.x) * t, py = c.a0.y + (c.b0.y - c.a0.y) * t;
     r.uv[2 * k] = (c.a0.z + (c.b0.z - c.a0.z) * t) * fc.tsx + fc.tox;
     r.uv[2 * k + 1] = (c.a0.w + (c.b0.w - c.a0.w) * t) * fc.tsy + fc.toy;
-    r.rrel[k] = c.a1.x + (c.b1.x - c.a1.x) * t;
+    r.rs[k] = ((c.a1.x + (c.b1.x - c.a1.x) * t) - 1.0f) * kRampScale;
     r.refl[k] = c.a1.y + (c.b1.y - c.a1.y) * t;
     r.inten[k] = c.a1.z + (c.b1.z - c.a1.z) * t;
     r.q[2 * k] = cvt_rz_sat(px * (float)S);
@@ -338,8 +342,8 @@ __device__ __forceinline__ bool zero_record(const RasterParams& p, const Rec& r,
     const float4 rf = ld4(r.refl);
     if (isnan(rf.x) || isnan(rf.y) || isnan(rf.z) || isnan(rf.w)) return true;
     if (p.S != 1 || !safe || r.bb[1] - r.bb[0] >= 4096 || r.bb[3] - r.bb[2] >= 4096) return false;
-    const float4 rl = ld4(r.rrel);
-    if (!(rl.x >= 1.0f && rl.y >= 1.0f && rl.z >= 1.0f && rl.w >= 1.0f)) return false;
+    const float4 rl = ld4(r.rs);  // rrel >= 1 exactly when the ramp is <= 0
+    if (!(rl.x <= 0.0f && rl.y <= 0.0f && rl.z <= 0.0f && rl.w <= 0.0f)) return false;
     const int* q = r.q;
     bool convex = true;
 #pragma unroll
@@ -540,8 +544,9 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
             float r0 = acc[(3 * blk) * 32 + lane];
             float r1 = acc[(3 * blk + 1) * 32 + lane];
             float r2 = acc[(3 * blk + 2) * 32 + lane];
+            // (no warp-wide operation below: lanes outside the image skip the records)
 #pragma unroll
-            for (int m = 0; m < kBatchRecords / 32; m++) {
+            for (int m = 0; m < kBatchRecords / 32 && in_image; m++) {
                 unsigned bits = sel[m];
                 while (bits) {  // in increasing record order: the reference's summation order
                     const int b = __ffs(bits) - 1;
@@ -550,7 +555,6 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                     bits &= bits - 1;
                     const Rec& r = recs[j];
                     RF_STAT(if (lane == 0) { st_iter++; st_whole += is_whole; })
-                    if (!in_image) continue;
                     int hits = S;
                     if (!is_whole) {
                         // (a bounds test first would save nothing: the block was selected
@@ -852,9 +856,8 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         const float v = wt[0] * uv01.y + wt[1] * uv01.w + wt[2] * uv23.y + wt[3] * uv23.w;
                         float dgu, dgv;
                         const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u, v, dgu, dgv);
-                        const float4 rl = ld4(r.rrel);
-                        const float rr = wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w;
-                        const float st = clampf((rr - 1.0f) * (1.0f / (0.95f - 1.0f)), 0.0f, 1.0f);
+                        const float4 rl = ld4(r.rs);
+                        const float st = __saturatef(wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w);
                         const float ri = st * st * (3.0f - 2.0f * st);
                         const float dri = (st > 0.0f && st < 1.0f) ? 6.0f * st * (1.0f - st) * (1.0f / (0.95f - 1.0f))
                                                                   : 0.0f;
@@ -951,7 +954,7 @@ __global__ void __launch_bounds__(256) k_raster_masks(const float4* __restrict__
                         const float px = a0.x + (b0.x - a0.x) * sub_pos, py = a0.y + (b0.y - a0.y) * sub_pos;
                         r.uv[2 * c] = (a0.z + (b0.z - a0.z) * sub_pos) * fc.tsx + fc.tox;
                         r.uv[2 * c + 1] = (a0.w + (b0.w - a0.w) * sub_pos) * fc.tsy + fc.toy;
-                        r.rrel[c] = a1.x + (b1.x - a1.x) * sub_pos;
+                        r.rs[c] = ((a1.x + (b1.x - a1.x) * sub_pos) - 1.0f) * kRampScale;
                         r.refl[c] = a1.y + (b1.y - a1.y) * sub_pos;
                         r.inten[c] = a1.z + (b1.z - a1.z) * sub_pos;
                         r.q[2 * c] = cvt_rz_sat(px * (float)S);
