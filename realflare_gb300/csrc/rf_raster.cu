@@ -64,7 +64,10 @@ __device__ unsigned long long g_raster_stats[5];
 #endif
 
 // Every group the shading loop reads starts on a 16-byte boundary and is read with
-// 16-byte shared-memory loads (ec[12..14] and flags as one vector).
+// 16-byte shared-memory loads (ec[12..14] and flags as one vector). Records are 272 bytes
+// apart (17 x 16): where the lanes of a warp read 32 different records at one offset (the
+// block selection), each group of 8 lanes then reads 8 different 16-byte bank groups instead
+// of one.
 struct alignas(16) Rec {
     int bb[4];       // xmin, xmax, ymin, ymax
     float col[4];    // the record's XYZ weight (1, 1, 1 with one wavelength), pad
@@ -76,8 +79,9 @@ struct alignas(16) Rec {
     int flags;       // 1: bounds rejection is exact; 2: adds nothing (collinear, or zero_record)
     int q[8];        // mixed vertex positions, sample space (x0, y0, ..., x3, y3)
     int color;       // w * WS + i
+    int pad[4];      // the stride
 };
-static_assert(sizeof(Rec) == 256 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0 &&
+static_assert(sizeof(Rec) == 272 && offsetof(Rec, bb) == 0 && offsetof(Rec, col) % 16 == 0 &&
                   offsetof(Rec, qf) % 16 == 0 && offsetof(Rec, uv) % 16 == 0 && offsetof(Rec, rs) % 16 == 0 &&
                   offsetof(Rec, inten) % 16 == 0 && offsetof(Rec, refl) % 16 == 0 &&
                   offsetof(Rec, ec) % 16 == 0 && offsetof(Rec, flags) == offsetof(Rec, ec) + 15 * sizeof(int),
@@ -137,10 +141,12 @@ __device__ __forceinline__ bool inside(const Rec& r, int px, int py) {
 // corners) agree, and then inside() is constant too. Returns 0 (no sample inside),
 // 2 (every sample inside) or 1 (mixed or undecided).
 __device__ __forceinline__ int rect_coverage(const Rec& r, int x0, int x1, int y0, int y1) {
+    int ec[16];
+    load_edges(r, ec);
     bool w[5];
 #pragma unroll
     for (int e = 0; e < 5; e++) {
-        const int A = r.ec[3 * e], B = r.ec[3 * e + 1], C = r.ec[3 * e + 2];
+        const int A = ec[3 * e], B = ec[3 * e + 1], C = ec[3 * e + 2];
         const int ay0 = A * y0, ay1 = A * y1, bx0 = B * x0, bx1 = B * x1;
         const int lo = C + min(ay0, ay1) + min(bx0, bx1);
         const int hi = C + max(ay0, ay1) + max(bx0, bx1);
@@ -525,7 +531,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                 bool take = false, all = false;
                 if (j < n_rec) {
                     const Rec& r = recs[j];
-                    const int flags = r.flags;
+                    const int flags = ld4i(r.ec + 12).w;  // with ec[12..14], which rect_coverage reads
                     if (!(flags & 2)) {  // collinear (intersect_quad rejects all) or all-zero
                         const int4 bb = *reinterpret_cast<const int4*>(r.bb);
                         take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);
@@ -809,7 +815,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                 bool take = false, all = false;
                 if (j < n_rec) {
                     const Rec& r = recs[j];
-                    const int flags = r.flags;
+                    const int flags = ld4i(r.ec + 12).w;  // with ec[12..14], which rect_coverage reads
                     if (!(flags & 2)) {
                         const int4 bb = *reinterpret_cast<const int4*>(r.bb);
                         take = !(flags & 1) || !(bx1 < bb.x || bx0 > bb.y || by1 < bb.z || by0 > bb.w);

@@ -8,15 +8,16 @@ from realflare_gb300 import prepare, synthetic
 from realflare_gb300.data import QSize
 
 
-def reduced(name: str, grid: int | None = None, resolution: int | None = None, paths: int | None = None,
+def reduced(name: str, grid: int | None = None, resolution: int | tuple | None = None, paths: int | None = None,
             wavelengths: int | None = None, integer_wavelengths: bool = True):
-    """A named workload with optional smaller grid / image / path list / wavelength count."""
+    """A named workload with optional smaller grid / image (side, or (width, height)) / path
+    list / wavelength count."""
     w = synthetic.workload(name, integer_wavelengths=integer_wavelengths)
     p = w.project
     if grid:
         p.render.grid_count = grid
     if resolution:
-        p.render.resolution = QSize(resolution, resolution)
+        p.render.resolution = QSize(*resolution) if isinstance(resolution, tuple) else QSize(resolution, resolution)
     if paths:
         w.paths = w.paths[:paths]
         p.flare.lens.ghost_paths = tuple(tuple(x) for x in w.paths)

@@ -32,6 +32,8 @@ WORKLOADS = {
     'plain-8': dict(),
     'spectral-16-small': dict(name='spectral-16', grid=24, resolution=256, paths=40, wavelengths=5),
     'production-24-small': dict(name='production-24', grid=16, resolution=256, paths=30, wavelengths=4),
+    # an image whose sides are not multiples of the 8-pixel blocks or the tiles
+    'spectral-16-ragged': dict(name='spectral-16', grid=20, resolution=(203, 117), paths=24, wavelengths=3),
 }
 
 
