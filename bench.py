@@ -558,8 +558,12 @@ def main() -> None:
         'traffic': traffic,
         'algorithmic_bytes': alg_bytes,
         'fragments_per_s': fragments / raster_s if fragments else None,
+        # the bound that limits this kernel: instruction issue (ncu on the reduced case)
+        'issue_active': prof.get('issue_active_small'),
         'note': ('issue-bound per-fragment shading (mean-value weights, bilinear ghost lookup per covered '
-                 'pixel x record); the vertex reads hit L2, so DRAM traffic is far below the algorithmic bytes'),
+                 'pixel x record): issue_active is the fraction of cycles the warp schedulers issue an '
+                 'instruction (ncu smsp__issue_active, 1024^2 / 48-ghost case of the same kernel); the vertex '
+                 'reads hit L2, so DRAM traffic is far below the algorithmic bytes'),
     }
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
