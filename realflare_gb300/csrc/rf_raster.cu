@@ -56,8 +56,10 @@ constexpr int kBatchRecords = RF_RASTER_BATCH;
 #ifdef RF_RASTER_STATS
 // Work counters of the statistics build (never compiled into the product library):
 // record iterations per 8 x 4 block, those of whole-block records, fragments, fragments of
-// whole-block records, block visits.
-__device__ unsigned long long g_raster_stats[5];
+// whole-block records, block visits, fragments whose smoothstep factor is 0 (rrel >= 1),
+// record iterations where that holds for every shaded pixel of the block.
+constexpr int kRasterStats = 7;
+__device__ unsigned long long g_raster_stats[kRasterStats];
 #define RF_STAT(stmt) stmt
 #else
 #define RF_STAT(stmt)
@@ -449,7 +451,8 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
     const int S = kS ? kS : p.S;
     const FragmentConsts fc = fcs;
     RF_STAT(unsigned long long st_iter = 0; unsigned long long st_whole = 0; unsigned long long st_frag = 0;
-            unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0;)
+            unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0; unsigned long long st_zero = 0;
+            unsigned long long st_zero_iter = 0;)
     // accumulators of the pixel blocks, [block * 3 + channel][lane]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
@@ -572,6 +575,13 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                     RF_STAT(st_frag++; st_frag_whole += is_whole;)
                     float wt[4];
                     barycentric_fast(r, (float)(sx0 + S / 2), (float)(sy0 + S / 2), wt);
+                    RF_STAT({
+                        const float4 rl = ld4(r.rs);
+                        const bool z = wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w <= 0.0f;
+                        st_zero += z;
+                        const unsigned am = __activemask();
+                        if (__all_sync(am, z) && lane == __ffs(am) - 1) st_zero_iter++;
+                    })
                     const float f = fragment_fast(r, wt, ghost, p, fc, kS == 1 ? 1 : hits);
                     const float4 col = *reinterpret_cast<const float4*>(r.col);
                     r0 += col.x * f;
@@ -591,7 +601,8 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
 
     RF_STAT(atomicAdd(&g_raster_stats[0], st_iter); atomicAdd(&g_raster_stats[1], st_whole);
             atomicAdd(&g_raster_stats[2], st_frag); atomicAdd(&g_raster_stats[3], st_frag_whole);
-            atomicAdd(&g_raster_stats[4], st_blocks);)
+            atomicAdd(&g_raster_stats[4], st_blocks); atomicAdd(&g_raster_stats[5], st_zero);
+            atomicAdd(&g_raster_stats[6], st_zero_iter);)
     __syncthreads();  // every block's last batch is shaded
     const float scale = p.intensity / (float)(p.W * p.S * p.WS);
 #pragma unroll
@@ -1227,13 +1238,14 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
 
 #ifdef RF_RASTER_STATS
 // Statistics build only: read (and zero) the counters of the k_raster launches since the
-// last call. out: record iterations, whole-block record iterations, fragments, fragments of
-// whole-block records, block visits.
+// last call. out[7]: record iterations, whole-block record iterations, fragments, fragments
+// of whole-block records, block visits, fragments with a zero smoothstep factor, record
+// iterations where every shaded pixel has one.
 extern "C" int rf_raster_stats(unsigned long long* out) {
     using namespace rf;
     if (!out) return RF_ERR_INVALID_ARG;
-    RF_TRY(cuda_status(cudaMemcpyFromSymbol(out, g_raster_stats, sizeof(unsigned long long) * 5)));
-    const unsigned long long zero[5] = {0, 0, 0, 0, 0};
+    RF_TRY(cuda_status(cudaMemcpyFromSymbol(out, g_raster_stats, sizeof(unsigned long long) * kRasterStats)));
+    const unsigned long long zero[kRasterStats] = {};
     RF_TRY(cuda_status(cudaMemcpyToSymbol(g_raster_stats, zero, sizeof zero)));
     return RF_OK;
 }
