@@ -45,46 +45,88 @@ __device__ __forceinline__ void rot2(float& x, float& y, float angle) {
     y = ny;
 }
 
+// Per-sample terms of k_starburst that do not depend on the pixel, tabulated per CTA in
+// chunks of kStarburstChunk samples: the light's XYZW weight at the sample's spectral
+// position, the chromatic scale and the spectrum index.
+constexpr int kStarburstChunk = 256;
+struct StarburstSample {
+    float4 light;
+    float scale;
+    int sidx;
+};
+
 __global__ void __launch_bounds__(256) k_starburst(const float* __restrict__ spectrum,
                                                    const float* __restrict__ light, rf_starburst_args a,
                                                    float4* __restrict__ image) {
+    __shared__ StarburstSample tab[kStarburstChunk];
     const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
-    if (x >= a.width || y >= a.height) return;
+    const bool inside = x < a.width && y < a.height;  // (every thread takes part in the table fills)
     float nx, ny;
     ndc_of(x, y, a.width, a.height, nx, ny);
     nx = (nx - a.offset[0]) / fmaxf(a.scale[0], 1.17549435e-38f);
     ny = (ny - a.offset[1]) / fmaxf(a.scale[1], 1.17549435e-38f);
     const size_t plane = (size_t)a.spectrum_width * a.spectrum_height;
+    // With blur 0 the jitter radius is 0 * sqrt(noise) = 0 (noise in [0, 1)), and with
+    // rotation 0 and a non-negative weight the angle is +-0 * (1 - noise^weight) = +-0: the
+    // jitter and the rotation then leave the position unchanged and their noise is skipped.
+    const bool jitter = a.blur != 0.0f;
+    const bool rotate = a.rotation != 0.0f || !(a.rotation_weight >= 0.0f);
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     const float fx = (float)x, fy = (float)y;
-    for (int t = 0; t < a.samples; t++) {
-        const float step = (float)t / (float)a.samples;
-        const float wavelength = step * (float)(RF_LAMBDA_MAX - RF_LAMBDA_MIN) + (float)RF_LAMBDA_MIN;
-        const float seed = (float)(t * 4);
-        float px = nx, py = ny;
-        const float radius = a.blur * sqrtf(noise3(fx, fy, seed));
-        const float alpha = noise3(fx, fy, seed + 1.0f) * 2.0f * RF_MPI_F;
-        float sa, ca;
-        sincosf(alpha, &sa, &ca);
-        px += ca * radius;
-        py += sa * radius;
-        // chromatic scale 1 - (1 - lambda / 560) (LAMBDA_MID is an int in starburst.cl)
-        const float sc = fmaxf(1.0f - (1.0f - (wavelength / (float)RF_LAMBDA_MID)) * 1.0f, 1.17549435e-38f);
-        px = px / sc;
-        py = py / sc;
-        const float sign = noise3(fx, fy, seed + 2.0f) > 0.5f ? 1.0f : -1.0f;
-        const float angle = sign * a.rotation * (1.0f - powf(noise3(fx, fy, seed + 3.0f), a.rotation_weight));
-        rot2(px, py, angle);
-        const float u = px * 0.5f + 0.5f, v = py * 0.5f + 0.5f;
-        int sidx = 0;
-        if (a.spectrum_count > 1) {
-            const int k = cvt_rz_sat(floorf((wavelength - a.lambda_first) / a.lambda_step + 0.5f));
-            sidx = k < 0 ? 0 : (k >= a.spectrum_count ? a.spectrum_count - 1 : k);
+    for (int t0 = 0; t0 < a.samples; t0 += kStarburstChunk) {
+        const int n = min(kStarburstChunk, a.samples - t0);
+        __syncthreads();  // the previous chunk's table is no longer read
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int t = t0 + i;
+            const float step = (float)t / (float)a.samples;
+            const float wavelength = step * (float)(RF_LAMBDA_MAX - RF_LAMBDA_MIN) + (float)RF_LAMBDA_MIN;
+            StarburstSample e;
+            // chromatic scale 1 - (1 - lambda / 560) (LAMBDA_MID is an int in starburst.cl)
+            e.scale = fmaxf(1.0f - (1.0f - (wavelength / (float)RF_LAMBDA_MID)) * 1.0f, 1.17549435e-38f);
+            int sidx = 0;
+            if (a.spectrum_count > 1) {
+                const int k = cvt_rz_sat(floorf((wavelength - a.lambda_first) / a.lambda_step + 0.5f));
+                sidx = k < 0 ? 0 : (k >= a.spectrum_count ? a.spectrum_count - 1 : k);
+            }
+            e.sidx = sidx;
+            e.light = make_float4(sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, 0, step, 0.0f, false),
+                                  sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, 1, step, 0.0f, false),
+                                  sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, 2, step, 0.0f, false),
+                                  sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, 3, step, 0.0f, false));
+            tab[i] = e;
         }
-        const float fi = sample_linear(spectrum + sidx * plane, a.spectrum_width, a.spectrum_height, 1, 0, u, v, false);
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[c] += sample_linear(light, RF_SPECTRUM_WIDTH, 1, 4, c, step, 0.0f, false) * fi;
+        __syncthreads();
+        if (!inside) continue;
+        for (int i = 0; i < n; i++) {
+            const int t = t0 + i;
+            const StarburstSample e = tab[i];
+            const float seed = (float)(t * 4);
+            float px = nx, py = ny;
+            if (jitter) {
+                const float radius = a.blur * sqrtf(noise3(fx, fy, seed));
+                const float alpha = noise3(fx, fy, seed + 1.0f) * 2.0f * RF_MPI_F;
+                float sa, ca;
+                sincosf(alpha, &sa, &ca);
+                px += ca * radius;
+                py += sa * radius;
+            }
+            px = px / e.scale;
+            py = py / e.scale;
+            if (rotate) {
+                const float sign = noise3(fx, fy, seed + 2.0f) > 0.5f ? 1.0f : -1.0f;
+                const float angle = sign * a.rotation * (1.0f - powf(noise3(fx, fy, seed + 3.0f), a.rotation_weight));
+                rot2(px, py, angle);
+            }
+            const float u = px * 0.5f + 0.5f, v = py * 0.5f + 0.5f;
+            const float fi = sample_linear(spectrum + e.sidx * plane, a.spectrum_width, a.spectrum_height, 1, 0, u, v,
+                                           false);
+            acc[0] += e.light.x * fi;
+            acc[1] += e.light.y * fi;
+            acc[2] += e.light.z * fi;
+            acc[3] += e.light.w * fi;
+        }
     }
+    if (!inside) return;
 #pragma unroll
     for (int c = 0; c < 4; c++) acc[c] = acc[c] / (float)a.samples;
     if (!isnan(a.vignetting[0])) {
