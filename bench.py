@@ -621,7 +621,7 @@ def run_raster_stats(args) -> None:
     S.rf_raster.restype = ctypes.c_int
     S.rf_raster_stats.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
     S.rf_raster_stats.restype = ctypes.c_int
-    out = (ctypes.c_ulonglong * 7)()
+    out = (ctypes.c_ulonglong * 8)()
     assert S.rf_raster_stats(out) == 0
     r = frame.raster
     st = S.rf_raster(r._buffers['vertexes'].data_ptr(), r._buffers['tile_offsets'].data_ptr(),
@@ -630,14 +630,14 @@ def run_raster_stats(args) -> None:
     torch.cuda.synchronize()
     assert st == 0, st
     assert S.rf_raster_stats(out) == 0
-    it, whole, frag, frag_whole, blocks, frag_zero, iter_zero = (int(v) for v in out)
+    it, whole, frag, frag_whole, blocks, frag_zero, iter_zero, steps = (int(v) for v in out)
     h, wd = frame.flare.shape[:2]
     print(json.dumps({
         'raster_stats': {
             'tile_entries': frame.entries, 'block_visits': blocks, 'record_iterations': it,
             'whole_block_record_iterations': whole, 'fragments': frag, 'fragments_in_whole_blocks': frag_whole,
             'fragments_per_pixel': frag / (h * wd), 'lane_efficiency': frag / max(1, 32 * it),
-            'fragments_outside_housing': frag_zero, 'record_iterations_all_outside_housing': iter_zero,
+            'shading_steps': steps, 'step_lane_efficiency': frag / max(1, 32 * steps) if steps else None,
         },
         'config': {'workload': args.workload, 'image': f'{wd}x{h}', 'ghosts': frame.P},
     }), flush=True)

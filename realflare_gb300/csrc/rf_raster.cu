@@ -57,8 +57,9 @@ constexpr int kBatchRecords = RF_RASTER_BATCH;
 // Work counters of the statistics build (never compiled into the product library):
 // record iterations per 8 x 4 block, those of whole-block records, fragments, fragments of
 // whole-block records, block visits, fragments whose smoothstep factor is 0 (rrel >= 1),
-// record iterations where that holds for every shaded pixel of the block.
-constexpr int kRasterStats = 7;
+// record iterations where that holds for every shaded pixel of the block (those two with
+// more than one sample per pixel), warp steps of the one-sample shading loop.
+constexpr int kRasterStats = 8;
 __device__ unsigned long long g_raster_stats[kRasterStats];
 #define RF_STAT(stmt) stmt
 #else
@@ -452,7 +453,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
     const FragmentConsts fc = fcs;
     RF_STAT(unsigned long long st_iter = 0; unsigned long long st_whole = 0; unsigned long long st_frag = 0;
             unsigned long long st_frag_whole = 0; unsigned long long st_blocks = 0; unsigned long long st_zero = 0;
-            unsigned long long st_zero_iter = 0;)
+            unsigned long long st_zero_iter = 0; unsigned long long st_steps = 0;)
     // accumulators of the pixel blocks, [block * 3 + channel][lane]
     float* acc = blend + ((p.WS + 3) & ~3);
 #pragma unroll
@@ -554,8 +555,49 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
             float r1 = acc[(3 * blk + 1) * 32 + lane];
             float r2 = acc[(3 * blk + 2) * 32 + lane];
             // (no warp-wide operation below: lanes outside the image skip the records)
+            if constexpr (kS == 1) {
+                // One sample per pixel: every lane first marks the selected records that cover
+                // its pixel (whole-block records cover every pixel; the others are tested, in a
+                // loop that is the same for all lanes), then shades its own covered records in
+                // increasing order. A lane is not held up by records that miss its pixel, so a
+                // warp takes about as many shading steps as its busiest pixel has fragments.
+                unsigned cov[kBatchRecords / 32];
 #pragma unroll
-            for (int m = 0; m < kBatchRecords / 32 && in_image; m++) {
+                for (int m = 0; m < kBatchRecords / 32; m++) {
+                    unsigned c = whole[m], part = sel[m] & ~whole[m];
+                    while (part) {
+                        const int b = __ffs(part) - 1;
+                        part &= part - 1;
+                        if (inside(recs[m * 32 + b], sx0, sy0)) c |= 1u << b;
+                    }
+                    cov[m] = in_image ? c : 0u;
+                    RF_STAT(if (lane == 0) { st_iter += __popc(sel[m]); st_whole += __popc(whole[m]); })
+                }
+                const float fx = (float)sx0, fy = (float)sy0;
+                for (;;) {
+                    int j = -1;
+#pragma unroll
+                    for (int m = 0; m < kBatchRecords / 32; m++) {
+                        if (j < 0 && cov[m]) {
+                            j = m * 32 + __ffs(cov[m]) - 1;
+                            cov[m] &= cov[m] - 1;
+                        }
+                    }
+                    if (j < 0) break;
+                    const Rec& r = recs[j];
+                    RF_STAT(st_frag++; st_frag_whole += (whole[j >> 5] >> (j & 31)) & 1u;
+                            if (lane == __ffs(__activemask()) - 1) st_steps++;)
+                    float wt[4];
+                    barycentric_fast(r, fx, fy, wt);
+                    const float f = fragment_fast(r, wt, ghost, p, fc, 1);
+                    const float4 col = *reinterpret_cast<const float4*>(r.col);
+                    r0 += col.x * f;
+                    r1 += col.y * f;
+                    r2 += col.z * f;
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < kBatchRecords / 32 && in_image && kS != 1; m++) {
                 unsigned bits = sel[m];
                 while (bits) {  // in increasing record order: the reference's summation order
                     const int b = __ffs(bits) - 1;
@@ -602,7 +644,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
     RF_STAT(atomicAdd(&g_raster_stats[0], st_iter); atomicAdd(&g_raster_stats[1], st_whole);
             atomicAdd(&g_raster_stats[2], st_frag); atomicAdd(&g_raster_stats[3], st_frag_whole);
             atomicAdd(&g_raster_stats[4], st_blocks); atomicAdd(&g_raster_stats[5], st_zero);
-            atomicAdd(&g_raster_stats[6], st_zero_iter);)
+            atomicAdd(&g_raster_stats[6], st_zero_iter); atomicAdd(&g_raster_stats[7], st_steps);)
     __syncthreads();  // every block's last batch is shaded
     const float scale = p.intensity / (float)(p.W * p.S * p.WS);
 #pragma unroll
@@ -1238,9 +1280,10 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
 
 #ifdef RF_RASTER_STATS
 // Statistics build only: read (and zero) the counters of the k_raster launches since the
-// last call. out[7]: record iterations, whole-block record iterations, fragments, fragments
+// last call. out[8]: record iterations, whole-block record iterations, fragments, fragments
 // of whole-block records, block visits, fragments with a zero smoothstep factor, record
-// iterations where every shaded pixel has one.
+// iterations where every shaded pixel has one (those two with more than one sample per
+// pixel), warp steps of the one-sample shading loop.
 extern "C" int rf_raster_stats(unsigned long long* out) {
     using namespace rf;
     if (!out) return RF_ERR_INVALID_ARG;
