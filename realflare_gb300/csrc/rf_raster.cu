@@ -561,7 +561,8 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                 // loop that is the same for all lanes), then shades its own covered records in
                 // increasing order. A lane is not held up by records that miss its pixel, so a
                 // warp takes about as many shading steps as its busiest pixel has fragments.
-                unsigned cov[kBatchRecords / 32];
+                static_assert(kBatchRecords <= 64, "one 64-bit coverage mask per lane");
+                unsigned long long cov = 0;
 #pragma unroll
                 for (int m = 0; m < kBatchRecords / 32; m++) {
                     unsigned c = whole[m], part = sel[m] & ~whole[m];
@@ -570,20 +571,14 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                         part &= part - 1;
                         if (inside(recs[m * 32 + b], sx0, sy0)) c |= 1u << b;
                     }
-                    cov[m] = in_image ? c : 0u;
+                    cov |= (unsigned long long)c << (32 * m);
                     RF_STAT(if (lane == 0) { st_iter += __popc(sel[m]); st_whole += __popc(whole[m]); })
                 }
+                if (!in_image) cov = 0;
                 const float fx = (float)sx0, fy = (float)sy0;
-                for (;;) {
-                    int j = -1;
-#pragma unroll
-                    for (int m = 0; m < kBatchRecords / 32; m++) {
-                        if (j < 0 && cov[m]) {
-                            j = m * 32 + __ffs(cov[m]) - 1;
-                            cov[m] &= cov[m] - 1;
-                        }
-                    }
-                    if (j < 0) break;
+                while (cov) {
+                    const int j = __ffsll(cov) - 1;
+                    cov &= cov - 1;
                     const Rec& r = recs[j];
                     RF_STAT(st_frag++; st_frag_whole += (whole[j >> 5] >> (j & 31)) & 1u;
                             if (lane == __ffs(__activemask()) - 1) st_steps++;)
