@@ -745,6 +745,8 @@ __device__ __forceinline__ float ghost_sample_grad(const float* __restrict__ tex
 }
 
 constexpr int kGradAttrs = 5;  // per corner: u, v, rrel, reflectance, intensity
+// row stride of the backward's per-warp transpose buffers (floats)
+constexpr int kRedStride = 36;
 // vertex float of each attribute (pos.xy, uv.xy, rrel, reflectance, intensity, pad)
 __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6};
 
@@ -764,12 +766,14 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     constexpr int kBlocks = T * T / 32, kCols = T / 8;
     extern __shared__ float4 smem4[];
     Rec* recs = (Rec*)smem4;
-    float* xyz = (float*)(recs + kBatchRecords);
+    // per-warp transpose buffers of the 20 per-lane products: [product][lane], rows
+    // kRedStride floats apart (16-byte aligned, and 16-byte row reads by consecutive lanes
+    // fall in different bank groups)
+    float* red = (float*)(recs + kBatchRecords) + (threadIdx.x >> 5) * (4 * kGradAttrs * kRedStride);
+    float* xyz = (float*)(recs + kBatchRecords) + 8 * 4 * kGradAttrs * kRedStride;
     float* blend = xyz + 3 * p.maxW * p.WS;
     float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
     float* rgrad = grgb + 96 * kBlocks;                // [record][corner * 5 + attribute]
-    // per-warp transpose buffer of the 20 per-lane products (stride 21: conflict-free)
-    float* red = rgrad + kBatchRecords * 4 * kGradAttrs + (threadIdx.x >> 5) * (32 * 21);
     __shared__ int next_block;
     const int tile = blockIdx.x;
     const int tx = tile % p.ntx, ty = tile / p.ntx;
@@ -932,12 +936,20 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
 #pragma unroll
                     for (int c = 0; c < 4; c++)
 #pragma unroll
-                        for (int a = 0; a < kGradAttrs; a++) red[lane * 21 + c * kGradAttrs + a] = gw[a] * wt[c];
+                        for (int a = 0; a < kGradAttrs; a++) red[(c * kGradAttrs + a) * kRedStride + lane] = gw[a] * wt[c];
                     __syncwarp();
                     if (lane < 4 * kGradAttrs) {
-                        float sum = 0.0f;
-#pragma unroll 8
-                        for (int l = 0; l < 32; l++) sum += red[l * 21 + lane];
+                        const float4* row = reinterpret_cast<const float4*>(red + lane * kRedStride);
+                        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            const float4 v = row[q];
+                            s0 += v.x;
+                            s1 += v.y;
+                            s2 += v.z;
+                            s3 += v.w;
+                        }
+                        const float sum = (s0 + s1) + (s2 + s3);
                         if (sum != 0.0f) atomicAdd(&rgrad[j * 4 * kGradAttrs + lane], sum);
                     }
                     __syncwarp();
@@ -1245,7 +1257,7 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
     const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
-                        sizeof(float) * (96 * (T * T / 32) + kBatchRecords * 4 * kGradAttrs + 8 * 32 * 21);
+                        sizeof(float) * (96 * (T * T / 32) + kBatchRecords * 4 * kGradAttrs + 8 * 4 * kGradAttrs * kRedStride);
     const FragmentConsts fc = fragment_consts(p);
     const float4 *im = (const float4*)image, *gim = (const float4*)grad_image;
     const unsigned grid = (unsigned)(p.ntx * nty);
