@@ -73,6 +73,21 @@ def make_workload(args):
     return w
 
 
+def workload_config(w, world: int) -> dict:
+    """The line's config: the workload and its sizes (both arms report the same)."""
+    from realflare_gb300 import prepare
+
+    p = w.project
+    ti = prepare.trace_inputs(p)
+    a = ti.args
+    r, sr = p.render.resolution, p.render.starburst.resolution
+    return {
+        'workload': w.name, 'image': f'{r.width()}x{r.height()}', 'ghosts': a.path_count,
+        'wavelengths': a.wavelength_count, 'grid': a.grid_count, 'rays_per_frame': ti.ray_count,
+        'starburst_aperture': f'{sr.width()}x{sr.height()}', 'parallelism': f'replicas{world}',
+    }
+
+
 def dist_init():
     import torch
 
@@ -483,7 +498,7 @@ def run_reference(args, rank, world) -> None:
         'value': s['value'], 'unit': 'frames/s', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': 1e3 / s['value'], 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32', 'data': 'synthetic',
-        'config': {'workload': args.workload, 'rays_per_frame': cpu.n_rays},
+        'config': workload_config(w, args.gpus),
         'cpu_baseline': {k: s[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
         'e2e': {'value': s['value'], 'unit': 'frames/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'stage_seconds': s['stage_seconds'], 'rays_per_s': s['rays_per_s'],
@@ -576,13 +591,10 @@ def main() -> None:
             'value': fps, 'unit': 'frames/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {
-                'workload': args.workload, 'image': f'{wd}x{h}', 'ghosts': frame.P, 'wavelengths': frame.W,
-                'grid': frame.G, 'rays_per_frame': frame.n_rays, 'starburst_aperture': '512x512',
-                'parallelism': f'replicas{world}',
+            'config': dict(workload_config(w, world), **{
                 'l2': f'per-frame working set (rays {frame.rays.numel() * 4 / 1e9:.2f} GB, tile entries '
                       f'{entries * 4 / 1e9:.2f} GB) > L2 (129 MB): no flush needed',
-            },
+            }),
             'rays_per_s': frame.n_rays / (last['trace'] / 1e3) * world,
             'stage_ms': {k: round(v, 3) for k, v in last.items()},
             'tile_entries': entries,
