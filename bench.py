@@ -469,15 +469,24 @@ def load_peaks() -> tuple:
         return 6800.0, 'fallback'
 
 
-def raster_profile() -> dict:
-    """k_raster figures of the production frame from the committed ncu summary
-    (DRAM bytes of one launch, tile entries and fragments of that launch)."""
-    path = os.path.join(ROOT, 'profiles', 'k_raster_production-24.json')
+def raster_profile(kernel: str = 'k_raster') -> dict:
+    """Figures of a kernel on the production frame from its committed ncu summary
+    (k_raster: DRAM bytes of one launch, tile entries and fragments of that launch;
+    k_trace: issue-slot use on the reduced case)."""
+    path = os.path.join(ROOT, 'profiles', f'{kernel}_production-24.json')
     try:
         with open(path) as f:
             return json.load(f)
     except (OSError, ValueError):
         return {}
+
+
+def trace_interactions(ti) -> int:
+    """Surface interactions of a trace: per ray that reaches the sensor, the reference's
+    loop steps 1 + elements + 2 (b1 - b2) (raytracing.cl:258-352), summed over every ray."""
+    paths = ti.paths.astype('int64')
+    per_ray = 1 + ti.args.element_count + 2 * (paths[:, 0] - paths[:, 1])
+    return int(per_ray.sum()) * ti.args.wavelength_count * ti.args.grid_count ** 2
 
 
 def run_reference(args, rank, world) -> None:
@@ -562,6 +571,8 @@ def main() -> None:
     alg_bytes = entries * (4 + 4 * 64) + h * wd * 16
     achieved = alg_bytes / raster_s / 1e9
     prof = raster_profile()
+    trace_prof = raster_profile('k_trace')
+    interactions = trace_interactions(frame.ti)
     traffic = fragments = None
     if prof.get('workload') == args.workload and prof.get('tile_entries') == entries:
         # the summary was taken on this very launch (same workload, same tile entries)
@@ -596,6 +607,15 @@ def main() -> None:
                       f'{entries * 4 / 1e9:.2f} GB) > L2 (129 MB): no flush needed',
             }),
             'rays_per_s': frame.n_rays / (last['trace'] / 1e3) * world,
+            # k_trace: FP32 / issue-bound (no DRAM or tensor bound applies)
+            'trace': {
+                'rays_per_s': frame.n_rays / (last['trace'] / 1e3) * world,
+                'surface_interactions': interactions,
+                'surface_interactions_per_s': interactions / (last['trace'] / 1e3) * world,
+                'issue_active': trace_prof.get('issue_active_small'),
+                'note': ('interactions: 1 + elements + 2 (b1 - b2) loop steps per ray that reaches the sensor; '
+                         'issue_active: ncu smsp__issue_active of k_trace, 1024^2 / 48-ghost case'),
+            },
             'stage_ms': {k: round(v, 3) for k, v in last.items()},
             'tile_entries': entries,
             'e2e': e2e,
