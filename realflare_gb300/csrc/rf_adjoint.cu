@@ -22,6 +22,12 @@ namespace rf {
 namespace {
 
 constexpr int kAdjThreads = 128;
+// resident blocks per SM requested from the register allocator (6: 80 registers; the
+// per-ray step record already lives in local memory, and the few spills cost less than the
+// extra resident warps gain)
+#ifndef RF_ADJOINT_MIN_BLOCKS
+#define RF_ADJOINT_MIN_BLOCKS 6
+#endif
 constexpr int kAdjMaxElements = 32;
 constexpr int kAdjMaxSteps = 3 * kAdjMaxElements;
 constexpr int kAdjTableRows = 4;
@@ -211,7 +217,7 @@ __device__ void intersect_adjoint(V3 p, V3 d, const SmemElement& e, V3 gh, V3 gn
     gcenter += -gcz;
 }
 
-__global__ void __launch_bounds__(kAdjThreads) k_trace_adjoint(const rf_lens_element* __restrict__ elements,
+__global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_adjoint(const rf_lens_element* __restrict__ elements,
                                                               const int2* __restrict__ paths,
                                                               const float* __restrict__ wavelengths,
                                                               const __grid_constant__ TraceParams p,

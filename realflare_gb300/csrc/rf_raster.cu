@@ -765,16 +765,16 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                       float* __restrict__ grad_vtx) {
     constexpr int kBlocks = T * T / 32, kCols = T / 8;
     extern __shared__ float4 smem4[];
-    Rec* recs = (Rec*)smem4;
+    Rec* recbuf = (Rec*)smem4;  // two batches of records
     // per-warp transpose buffers of the 20 per-lane products: [product][lane], rows
     // kRedStride floats apart (16-byte aligned, and 16-byte row reads by consecutive lanes
     // fall in different bank groups)
-    float* red = (float*)(recs + kBatchRecords) + (threadIdx.x >> 5) * (4 * kGradAttrs * kRedStride);
-    float* xyz = (float*)(recs + kBatchRecords) + 8 * 4 * kGradAttrs * kRedStride;
+    float* red = (float*)(recbuf + 2 * kBatchRecords) + (threadIdx.x >> 5) * (4 * kGradAttrs * kRedStride);
+    float* xyz = (float*)(recbuf + 2 * kBatchRecords) + 8 * 4 * kGradAttrs * kRedStride;
     float* blend = xyz + 3 * p.maxW * p.WS;
     float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
-    float* rgrad = grgb + 96 * kBlocks;                // [record][corner * 5 + attribute]
-    __shared__ int next_block;
+    float* rgrad_buf = grgb + 96 * kBlocks;            // two batches of [record][corner * 5 + attribute]
+    __shared__ int next_block[2];
     const int tile = blockIdx.x;
     const int tx = tile % p.ntx, ty = tile / p.ntx;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -820,35 +820,52 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
         grgb[(3 * blk + 1) * 32 + lane] = g1;
         grgb[(3 * blk + 2) * 32 + lane] = g2;
     }
-    for (int i = threadIdx.x; i < kBatchRecords * 4 * kGradAttrs; i += kThreads) rgrad[i] = 0.0f;
+    for (int i = threadIdx.x; i < 2 * kBatchRecords * 4 * kGradAttrs; i += kThreads) rgrad_buf[i] = 0.0f;
 
     const int S = kS ? kS : p.S;
     const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
     const int per_batch = kBatchRecords / p.WS;
     const int my_entry = threadIdx.x >> 2, my_corner = threadIdx.x & 3;
     const int Q = (p.G - 1) * (p.G - 1), VC = p.G * p.G;
-    for (uint32_t base = begin; base < end; base += per_batch) {
-        const int n_rec = (int)min((uint32_t)per_batch, end - base) * p.WS;
-        __syncthreads();  // blend, colours and pixel gradients set; the previous batch flushed
+    // Records of the batch at `first` into buffer `dst`, as k_raster builds them: thread j
+    // loads and mixes corner j % 4 of entry j / 4 (the four corners of an entry sit in one
+    // warp), then one thread per record finishes it. Batches are double-buffered: warps that
+    // are done shading batch t build batch t + 1 while the others shade, one barrier per
+    // batch, and each batch sums its records' gradients in its own buffer.
+    auto build = [&](Rec* dst, uint32_t first) {
         for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
             const int e = my_entry + 64 * h;
-            if (e < per_batch && base + e < end) {
+            if (e < per_batch && first + e < end) {
                 CornerLoad c;
-                load_corner(vtx, tile_entries[base + e], my_corner, p, c);
-                for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, fc, recs[e * p.WS + i]);
+                load_corner(vtx, tile_entries[first + e], my_corner, p, c);
+                for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, fc, dst[e * p.WS + i]);
             }
         }
-        __syncthreads();
-        for (int j = threadIdx.x; j < n_rec; j += kThreads) {
-            const uint32_t entry = tile_entries[base + j / p.WS];
-            finish_record(p, (int)(entry % p.maxW), j % p.WS, xyz, recs[j]);
+        __syncwarp();  // the four corners of each record are stored
+        for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
+            const int e = my_entry + 64 * h;
+            if (e < per_batch && first + e < end) {
+                const uint32_t entry = tile_entries[first + e];
+                for (int i = my_corner; i < p.WS; i += 4) finish_record(p, (int)(entry % p.maxW), i, xyz, dst[e * p.WS + i]);
+            }
         }
-        if (threadIdx.x == 0) next_block = 0;
-        __syncthreads();
+    };
+    if (threadIdx.x == 0) {
+        next_block[0] = 0;
+        next_block[1] = 0;
+    }
+    __syncthreads();  // blend weights, colours and pixel gradients are set
+    if (begin < end) build(recbuf, begin);
+    __syncthreads();
+    int cur = 0;
+    for (uint32_t base = begin; base < end; base += per_batch, cur ^= 1) {
+        const int n_rec = (int)min((uint32_t)per_batch, end - base) * p.WS;
+        const Rec* recs = recbuf + cur * kBatchRecords;
+        float* rgrad = rgrad_buf + cur * (kBatchRecords * 4 * kGradAttrs);
 #pragma unroll 1
         for (;;) {
             int blk = 0;
-            if (lane == 0) blk = atomicAdd(&next_block, 1);
+            if (lane == 0) blk = atomicAdd(&next_block[cur], 1);
             blk = __shfl_sync(0xffffffffu, blk, 0);
             if (blk >= kBlocks) break;
             const int x0 = tx * T + (blk % kCols) * 8, y0 = ty * T + (blk / kCols) * 4;
@@ -956,8 +973,13 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                 }
             }
         }
-        __syncthreads();
-        // each record's gradients to the two vertices of each corner (mix_vertex weights)
+        if (base + per_batch < end) build(recbuf + (cur ^ 1) * kBatchRecords, base + per_batch);
+        // the other counter was last used by the previous batch, behind the last barrier
+        if (threadIdx.x == 0) next_block[cur ^ 1] = 0;
+        __syncthreads();  // every block of this batch is shaded and the next batch is built
+        // each record's gradients to the two vertices of each corner (mix_vertex weights);
+        // the buffer is cleared here and written again two batches later, behind the next
+        // barrier
         for (int idx = threadIdx.x; idx < n_rec * 4 * kGradAttrs; idx += kThreads) {
             const float g = rgrad[idx];
             if (g == 0.0f) continue;
@@ -1256,8 +1278,9 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     p.T = T;
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
-    const size_t smem = sizeof(Rec) * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
-                        sizeof(float) * (96 * (T * T / 32) + kBatchRecords * 4 * kGradAttrs + 8 * 4 * kGradAttrs * kRedStride);
+    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
+                        sizeof(float) * (96 * (T * T / 32) + 2 * kBatchRecords * 4 * kGradAttrs +
+                                         8 * 4 * kGradAttrs * kRedStride);
     const FragmentConsts fc = fragment_consts(p);
     const float4 *im = (const float4*)image, *gim = (const float4*)grad_image;
     const unsigned grid = (unsigned)(p.ntx * nty);

@@ -91,7 +91,35 @@ class LensParameters:
         return [self.radii, self.gaps, self.thickness, self.light]
 
     def elements(self, radii, gaps, thickness, light, n_elements: int):
-        """(radius, center, thickness, direction.xyz) per element as torch tensors."""
+        """(radius, center, thickness, direction.xyz) per element as torch tensors.
+
+        The map is affine in the parameters, so it is evaluated as one matrix-vector product
+        (and torch differentiates it as one): the matrix and offset come from
+        ``elements_direct`` (the map's definition) at the zero and unit parameter vectors,
+        once per element count, device and dtype."""
+        M, b = self._affine(n_elements, radii.device, radii.dtype)
+        out = torch.addmv(b, M, torch.cat([radii, gaps, thickness, light]))
+        n = n_elements
+        return out[:n], out[n:2 * n], out[2 * n:3 * n], out[3 * n:3 * n + 3]
+
+    def _affine(self, n_elements: int, device, dtype):
+        key = (n_elements, str(device), dtype)
+        cache = self.__dict__.setdefault('_affine_cache', {})
+        if key not in cache:
+            sizes = [self.radii.numel(), self.gaps.numel(), self.thickness.numel(), 2]
+
+            def f(vec):
+                r, g, t, l = torch.split(vec, sizes)
+                return torch.cat(self.elements_direct(r, g, t, l, n_elements))
+
+            zero = torch.zeros(sum(sizes), dtype=torch.float64)
+            b = f(zero)
+            M = torch.stack([f(e) - b for e in torch.eye(sum(sizes), dtype=torch.float64)], dim=1)
+            cache[key] = (M.to(device=device, dtype=dtype), b.to(device=device, dtype=dtype))
+        return cache[key]
+
+    def elements_direct(self, radii, gaps, thickness, light, n_elements: int):
+        """The map itself, op by op: (radius, center, thickness, direction.xyz)."""
         lo = self.layout
         dev, dt = radii.device, radii.dtype
         radius = torch.zeros(n_elements, device=dev, dtype=dt)

@@ -174,3 +174,29 @@ def test_hash_sine_reduction():
     # |r| reach 3 pi/4; sincosf stays accurate there, only the quadrant has to match k
     assert np.abs(np.float64(r)).max() < 3 * np.pi / 4
     assert np.abs(got - want).max() < 4e-7
+
+
+def test_lens_parameter_map_equals_its_direct_form():
+    """LensParameters.elements (one matrix-vector product) equals elements_direct (the map
+    op by op) in value and in gradient, on parameters away from the lens's own."""
+    import torch
+
+    from realflare_gb300 import synthetic
+    from realflare_gb300.diff import LensParameters
+
+    w = synthetic.workload('differentiable-16')
+    lp = LensParameters(w.project, device='cpu')
+    n = len(w.project.flare.lens.lens_model.lens_elements) + 1  # with the sensor
+    g = torch.Generator().manual_seed(0)
+    base = [t + torch.randn(t.shape, generator=g, dtype=torch.float64) * 0.1 * (t.abs() + 1) for t in lp.tensors()]
+    weights = [torch.randn(k, generator=g, dtype=torch.float64) for k in (n, n, n, 3)]
+    grads = []
+    for fn in (lp.elements, lp.elements_direct):
+        ps = [t.clone().requires_grad_(True) for t in base]
+        out = fn(*ps, n)
+        loss = sum((o * wt).sum() for o, wt in zip(out, weights))
+        loss.backward()
+        grads.append(([o.detach() for o in out], [p.grad for p in ps]))
+    (va, ga), (vb, gb) = grads
+    for x, y in zip(va + ga, vb + gb):
+        assert torch.allclose(x, y, rtol=1e-12, atol=1e-12)
