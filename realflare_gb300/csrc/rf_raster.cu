@@ -747,6 +747,8 @@ __device__ __forceinline__ float ghost_sample_grad(const float* __restrict__ tex
 constexpr int kGradAttrs = 5;  // per corner: u, v, rrel, reflectance, intensity
 // row stride of the backward's per-warp transpose buffers (floats)
 constexpr int kRedStride = 36;
+// rows of a warp's transpose buffer: the 5 attribute gradients and the 4 corner weights
+constexpr int kRedRows = kGradAttrs + 4;
 // vertex float of each attribute (pos.xy, uv.xy, rrel, reflectance, intensity, pad)
 __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6};
 
@@ -766,11 +768,11 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     constexpr int kBlocks = T * T / 32, kCols = T / 8;
     extern __shared__ float4 smem4[];
     Rec* recbuf = (Rec*)smem4;  // two batches of records
-    // per-warp transpose buffers of the 20 per-lane products: [product][lane], rows
-    // kRedStride floats apart (16-byte aligned, and 16-byte row reads by consecutive lanes
-    // fall in different bank groups)
-    float* red = (float*)(recbuf + 2 * kBatchRecords) + (threadIdx.x >> 5) * (4 * kGradAttrs * kRedStride);
-    float* xyz = (float*)(recbuf + 2 * kBatchRecords) + 8 * 4 * kGradAttrs * kRedStride;
+    // per-warp transpose buffers of each lane's 5 attribute gradients and 4 corner weights:
+    // [row][lane], rows kRedStride floats apart (16-byte aligned, and the rows that lanes read
+    // side by side fall in different bank groups)
+    float* red = (float*)(recbuf + 2 * kBatchRecords) + (threadIdx.x >> 5) * (kRedRows * kRedStride);
+    float* xyz = (float*)(recbuf + 2 * kBatchRecords) + 8 * kRedRows * kRedStride;
     float* blend = xyz + 3 * p.maxW * p.WS;
     float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
     float* rgrad_buf = grgb + 96 * kBlocks;            // two batches of [record][corner * 5 + attribute]
@@ -948,23 +950,26 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         gw[3] = ci_raw > 0.0f ? d * gi * ri * ai : 0.0f;
                         gw[4] = ai_raw > 0.0f ? d * gi * ri * ci : 0.0f;
                     }
-                    // the warp's sum of each corner attribute's gradient: every lane writes its
-                    // 20 products, lane k < 20 adds up column k
+                    // the warp's sum of each corner attribute's gradient, sum over lanes of
+                    // gw[a] * wt[c]: every lane writes its 5 attribute gradients and 4 weights
+                    // (rows 0-4 and 5-8), lane k < 20 forms column (a, c) = (k % 5, k / 5)
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
+                    for (int a = 0; a < kGradAttrs; a++) red[a * kRedStride + lane] = gw[a];
 #pragma unroll
-                        for (int a = 0; a < kGradAttrs; a++) red[(c * kGradAttrs + a) * kRedStride + lane] = gw[a] * wt[c];
+                    for (int c = 0; c < 4; c++) red[(kGradAttrs + c) * kRedStride + lane] = wt[c];
                     __syncwarp();
                     if (lane < 4 * kGradAttrs) {
-                        const float4* row = reinterpret_cast<const float4*>(red + lane * kRedStride);
+                        const int a = lane % kGradAttrs, c = lane / kGradAttrs;
+                        const float4* ga = reinterpret_cast<const float4*>(red + a * kRedStride);
+                        const float4* wc = reinterpret_cast<const float4*>(red + (kGradAttrs + c) * kRedStride);
                         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
 #pragma unroll
                         for (int q = 0; q < 8; q++) {
-                            const float4 v = row[q];
-                            s0 += v.x;
-                            s1 += v.y;
-                            s2 += v.z;
-                            s3 += v.w;
+                            const float4 g = ga[q], v = wc[q];
+                            s0 = fmaf(g.x, v.x, s0);
+                            s1 = fmaf(g.y, v.y, s1);
+                            s2 = fmaf(g.z, v.z, s2);
+                            s3 = fmaf(g.w, v.w, s3);
                         }
                         const float sum = (s0 + s1) + (s2 + s3);
                         if (sum != 0.0f) atomicAdd(&rgrad[j * 4 * kGradAttrs + lane], sum);
@@ -1280,7 +1285,7 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     const int nty = (p.height + T - 1) / T;
     const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
                         sizeof(float) * (96 * (T * T / 32) + 2 * kBatchRecords * 4 * kGradAttrs +
-                                         8 * 4 * kGradAttrs * kRedStride);
+                                         8 * kRedRows * kRedStride);
     const FragmentConsts fc = fragment_consts(p);
     const float4 *im = (const float4*)image, *gim = (const float4*)grad_image;
     const unsigned grid = (unsigned)(p.ntx * nty);
