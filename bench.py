@@ -57,6 +57,8 @@ def parse_args():
                     help='skip the DIAGRAM element measurement (trace with hits and drawing)')
     ap.add_argument('--raster-stats', action='store_true',
                     help='count k_raster work (statistics build of the library) instead of timing')
+    ap.add_argument('--differentiable-only', action='store_true',
+                    help='only the forward+adjoint measurement of the 16-surface lens (for profiler captures)')
     return ap.parse_args()
 
 
@@ -524,6 +526,9 @@ def main() -> None:
         return
     if args.raster_stats:
         run_raster_stats(args)
+        return
+    if args.differentiable_only:
+        print(json.dumps({'differentiable': run_differentiable(args)}), flush=True)
         return
     import torch
 
