@@ -4,7 +4,9 @@
 // the chunk sums. Radix sort: 8-bit digits; per pass a block histogram, a scan of the
 // (digit, block) counts in digit-major order, and a stable scatter in which each warp
 // ranks its items in input order with __match_any_sync and the warps' counts are
-// prefixed per digit. Stability makes the output ordered by (key, input position).
+// prefixed per digit; the block stages its chunk in shared memory in (digit, input) order
+// and writes each digit's run with consecutive threads. Stability makes the output ordered
+// by (key, input position).
 #include "rf_common.cuh"
 
 namespace rf {
@@ -105,6 +107,8 @@ __global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* __re
                                                             uint32_t* __restrict__ keys_out,
                                                             uint32_t* __restrict__ vals_out) {
     __shared__ uint32_t warp_count[kWarps][257];
+    __shared__ uint32_t stage_k[kChunk], stage_v[kChunk];  // the chunk in (digit, input) order
+    __shared__ uint32_t digit_start[256], digit_out[256], warp_sums[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kWarps * 257; i += kThreads) (&warp_count[0][0])[i] = 0;
     __syncthreads();
@@ -132,26 +136,46 @@ __global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* __re
         __syncwarp();
     }
     __syncthreads();
-    // per digit: prefix over warps, then add the block's global offset
+    // per digit (thread d): prefix over warps, the block's count of the digit, and where its
+    // run starts in the block (a scan over digits) and in the output (the global offset)
     {
         const int d = threadIdx.x;  // 256 threads = 256 digits
-        uint32_t run = offsets[(size_t)d * nblocks + blockIdx.x];
+        uint32_t run = 0;
 #pragma unroll
         for (int w = 0; w < kWarps; w++) {
             uint32_t c = warp_count[w][d];
             warp_count[w][d] = run;
             run += c;
         }
+        const uint32_t start = block_exclusive_scan(run, warp_sums, nullptr);
+        digit_start[d] = start;
+        digit_out[d] = offsets[(size_t)d * nblocks + blockIdx.x];
     }
     __syncthreads();
+    // stage every item at its place in the block's digit-ordered chunk ...
 #pragma unroll
     for (int r = 0; r < kItems; r++) {
         long long i = wbase + (long long)r * 32 + lane;
         if (i < n) {
             uint32_t d = (key[r] >> shift) & 255u;
-            uint32_t pos = warp_count[warp][d] + rank[r];
-            keys_out[pos] = key[r];
-            vals_out[pos] = val[r];
+            uint32_t lp = digit_start[d] + warp_count[warp][d] + rank[r];
+            stage_k[lp] = key[r];
+            stage_v[lp] = val[r];
+        }
+    }
+    __syncthreads();
+    // ... and write the chunk out with consecutive threads on consecutive places of each run
+    const long long in_block = n - (long long)blockIdx.x * kChunk;
+    const int count = in_block < kChunk ? (int)in_block : kChunk;
+#pragma unroll
+    for (int r = 0; r < kItems; r++) {
+        const int lp = r * kThreads + threadIdx.x;
+        if (lp < count) {
+            const uint32_t k = stage_k[lp];
+            const uint32_t d = (k >> shift) & 255u;
+            const uint32_t pos = digit_out[d] + (uint32_t)lp - digit_start[d];
+            keys_out[pos] = k;
+            vals_out[pos] = stage_v[lp];
         }
     }
 }
