@@ -14,9 +14,9 @@ cannot run here through OpenCL (no platform). This recipe compiles the kernel so
    NDRange driver: one OpenMP loop over work-items per launch), and compiled with
    ``oracle/cl_shim.hpp`` (the OpenCL C built-ins in C++).
 
-The generated ``.cpp`` files and the library go to ``oracle/_ref/`` only (git-ignored, not
-gpurun-ignored), so a machine without the reference checkout can rebuild the library from
-the generated sources (``build(reference=None)``).
+The generated ``.cpp`` files and the library go to ``oracle/_ref/`` only (kept out of version
+control, but copied with the working tree), so a machine without the reference checkout can
+rebuild the library from the generated sources (``build(reference=None)``).
 """
 from __future__ import annotations
 
