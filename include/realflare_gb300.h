@@ -267,9 +267,10 @@ int rf_ghost_frft(const float* aperture, int32_t width, int32_t height, float al
  * its own pool, or a render loop that must not allocate after start-up (an allocation can
  * synchronise the device and stall a frame), passes only the aperture and the texture;
  * the scratch is a static device array of 3 x RF_GHOST_FRFT_STATIC_MAX_PIXELS complex64
- * values (6 MiB) that every GPU loading this library holds until the process exits. The
- * first call on a device looks up the array's device address, so make that first call
- * before any stream capture. All calls share the array: calls that overlap on the GPU
+ * values (6 MiB) that every GPU loading this library holds until the process exits. Every
+ * call looks up the array's device address on the current device (so no address outlives
+ * a device reset); the first call on a device may load the library's device code, so make
+ * that first call before any stream capture. All calls share the array: calls that overlap on the GPU
  * (other streams, other host threads on the same device) race. Sizes above the maximum
  * return RF_ERR_INVALID_ARG (text via rf_last_cuda_error). Allocates nothing. */
 int rf_ghost_frft_static(const float* aperture, int32_t width, int32_t height, float alpha,

@@ -17,6 +17,9 @@ cannot run here through OpenCL (no platform). This recipe compiles the kernel so
 The generated ``.cpp`` files and the library go to ``oracle/_ref/`` only (kept out of version
 control, but copied with the working tree), so a machine without the reference checkout can
 rebuild the library from the generated sources (``build(reference=None)``).
+
+The checkout is the ``reference`` argument, else the ``REALFLARE_REFERENCE`` environment
+variable; without either, previously generated sources are compiled.
 """
 from __future__ import annotations
 
@@ -28,7 +31,6 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, '_ref')
 LIB = os.path.join(OUT, 'librf_ref.so')
-DEFAULT_REFERENCE = '/root/reference'
 
 _VEC_LITERAL = re.compile(r'\(\s*(u?(?:char|short|int|long|float|double)(?:2|3|4|8|16))\s*\)\s*\(')
 
@@ -101,10 +103,11 @@ def generate(reference: str) -> list:
     return files
 
 
-def build(reference: str | None = DEFAULT_REFERENCE, force: bool = False) -> str | None:
+def build(reference: str | None = None, force: bool = False) -> str | None:
     """Generate (when the reference checkout exists) and compile. Returns the library path,
     or None when neither the reference nor previously generated sources are available."""
     sources = [os.path.join(OUT, f'ref_{n}.cpp') for n in PROGRAMS]
+    reference = reference or os.environ.get('REALFLARE_REFERENCE')
     if reference and os.path.isdir(reference):
         sources = generate(reference)
     elif not all(os.path.exists(s) for s in sources):
@@ -128,4 +131,4 @@ def build(reference: str | None = DEFAULT_REFERENCE, force: bool = False) -> str
 
 
 if __name__ == '__main__':
-    print(build(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REFERENCE, force='--force' in sys.argv))
+    print(build(sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != '--force' else None, force='--force' in sys.argv))

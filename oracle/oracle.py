@@ -51,6 +51,7 @@ class Oracle:
             lib.rfo_bin_masks.argtypes = [_P, _I, _F, _I, _I, _I, _P]
             lib.rfo_raster.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P]
             lib.rfo_raster_rows.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P, _I, _I, _I, _I]
+            lib.rfo_raster_pixels.argtypes = [_P, _P, _I, _P, _P, ctypes.POINTER(RasterArgs), _P, _LL, _P]
             lib.rfo_aperture_shape.argtypes = [_P, _I, _I, _F, _F, _I, _F, _F, _F]
             lib.rfo_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
             lib.rfo_aperture_noise_dust.argtypes = [_P, _P, _I, _I, _F, _F]
@@ -140,6 +141,17 @@ class Oracle:
                                      _ptr(image), rows[0], rows[1], cols[0], cols[1])
         return image
 
+    def raster_pixels(self, vertexes, masks, ghost, spectrum, args: RasterArgs, xy, image=None):
+        """raster() of the listed pixels only ((n, 2) int x, y, unflipped), one parallel
+        region; returns the full-size image with those pixels set (others as given, or 0)."""
+        if image is None:
+            image = np.zeros((args.height, args.width, 4), np.float32)
+        xy = _c(xy, np.int32)
+        self.lib.rfo_raster_pixels(_ptr(_c(vertexes, np.float32)), _ptr(_c(masks, np.uint64)), masks.shape[1],
+                                   _ptr(_c(ghost, np.float32)), _ptr(_c(spectrum, np.float32)), ctypes.byref(args),
+                                   _ptr(xy), len(xy), _ptr(image))
+        return image
+
     def aperture_shape(self, w, h, size, blades, rotation, roundness, softness):
         out = np.zeros((h, w), np.float32)
         self.lib.rfo_aperture_shape(_ptr(out), w, h, size[0], size[1], blades, rotation, roundness, softness)
@@ -191,6 +203,10 @@ class Reference:
             lib.ref_binner.argtypes = [_P, _I, _F, _I, _I, _I, _I, _P]
             lib.ref_rasterizer.argtypes = [_P, _P, _I, _P, _I, _I, _P, _I, _I, _I, _I, _I, _F, _F, _I, _I, _I,
                                            _I, _I, _I, _I, _P]
+            lib.ref_rasterizer_pixels.argtypes = [_P, _P, _I, _P, _I, _I, _P, _I, _I, _I, _I, _I, _F, _F, _I, _I,
+                                                  _I, _P, _LL, _P]
+            lib.ref_set_threads.argtypes = [_I]
+            lib.ref_set_threads.restype = _I
             lib.ref_starburst.argtypes = [_P, _I, _I, _P, _I, _F, _F, _F, _P, _F, _P, _P, _I, _I, _I, _I, _P]
             lib.ref_aperture_shape.argtypes = [_P, _I, _I, _F, _F, _I, _F, _F, _F]
             lib.ref_aperture_dust.argtypes = [_P, _I, _I, _F, _F, _F, _F, _F, _F, _F, _F]
@@ -269,6 +285,24 @@ class Reference:
                                 args.intensity, args.ghost_scale, args.width, args.height, args.bin_size, y0, y1,
                                 cols[0], cols[1], _ptr(image))
         return image
+
+    def rasterizer_pixels(self, vertexes, masks, ghost, spectrum, args: RasterArgs, xy, image=None):
+        """The reference rasterizer on the listed pixels ((n, 2) int x, y, unflipped) in one
+        parallel region; returns the full-size image with those pixels set."""
+        if image is None:
+            image = np.zeros((args.height, args.width, 4), np.float32)
+        g = _c(ghost, np.float32)
+        xy = _c(xy, np.int32)
+        self.lib.ref_rasterizer_pixels(_ptr(_c(vertexes, np.float32)), _ptr(_c(masks, np.uint64)), masks.shape[1],
+                                       _ptr(g), g.shape[1], g.shape[0], _ptr(_c(spectrum, np.float32)),
+                                       args.path_count, args.wavelength_count, args.wavelength_sub_count,
+                                       args.grid_count, args.sub_steps, args.intensity, args.ghost_scale, args.width,
+                                       args.height, args.bin_size, _ptr(xy), len(xy), _ptr(image))
+        return image
+
+    def set_threads(self, threads: int) -> int:
+        """OpenMP threads of the reference kernels (0 keeps the count); returns the previous."""
+        return self.lib.ref_set_threads(threads)
 
     def starburst(self, fourier, spectrum, a: StarburstArgs, rows=None):
         out = np.zeros((a.height, a.width, 4), np.float32)

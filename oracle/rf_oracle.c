@@ -747,6 +747,37 @@ static void finish_pixel(const rf_raster_args* a, int x, int y, const real rgb[3
     }
 }
 
+/* rfo_raster on a list of pixels (x, y pairs, unflipped) in one OpenMP region: each listed
+ * pixel of the full-size image is cleared and shaded (sampled frames). */
+int rfo_raster_pixels(const float* vertexes, const uint64_t* masks, int batch_count, const float* ghost,
+                      const float* spectrum, const rf_raster_args* a, const int32_t* xy, long long count,
+                      float* image) {
+    const int B = a->bin_size;
+    const int bdx = (a->width + B - 1) / B;
+    const long long prim_total = (long long)a->path_count * (a->grid_count - 1) * (a->grid_count - 1);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long i = 0; i < count; i++) {
+        const int x = xy[2 * i], y = xy[2 * i + 1];
+        const int bin = (y / B) * bdx + (x / B);
+        real rgb[3] = {0, 0, 0};
+        for (int batch = 0; batch < batch_count; batch++) {
+            const uint64_t* q = masks + 4 * ((size_t)bin * batch_count + batch);
+            if ((q[0] & 1u) == 0) continue;
+            for (int k = 0; k < RF_BATCH_PRIMITIVE_COUNT; k++) {
+                long long prim = (long long)batch * RF_BATCH_PRIMITIVE_COUNT + k;
+                if (prim >= prim_total) continue;
+                int bit = k + 1;
+                if (!((q[bit >> 6] >> (bit & 63)) & 1u)) continue;
+                shade_prim(vertexes, prim, a, ghost, spectrum, x, y, rgb);
+            }
+        }
+        float* out = image + 4 * ((size_t)(a->height - (y + 1)) * a->width + x);
+        out[0] = out[1] = out[2] = out[3] = 0;
+        finish_pixel(a, x, y, rgb, image);
+    }
+    return 0;
+}
+
 /* Fragments (covered pixel x primitive x wavelength pair x sub-wavelength) of the
  * rasterizer, in its loop order, with their hit counts and mean-value weights: the frozen
  * coverage of finite-difference checks of the render's derivative. Writes at most capacity

@@ -273,29 +273,17 @@ extern "C" int rf_ghost_frft(const float* aperture, int32_t width, int32_t heigh
 // rf_ghost_frft_static keeps its scratch in this file-scope device array instead of a
 // caller buffer. Every GPU that loads the library holds the array (6 MiB) until the
 // process exits; all calls share it.
-#include <mutex>
-
 static __device__ __align__(256) float2 g_ghost_frft_scratch[3 * RF_GHOST_FRFT_STATIC_MAX_PIXELS];
 
 namespace rf {
 namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_static_mutex;
-float* g_static_scratch[kMaxDevices] = {};
-
-// Device address of the static scratch on the current device, looked up on the first
-// call for each device (the host-side symbol is not a device address).
+// Device address of the static scratch on the current device. The host-side symbol is
+// not a device address; the lookup runs on every call (it is cheap), so a pointer is
+// never kept across a device reset, after which the module and its array are reloaded.
 int static_scratch(float** out) {
-    int dev = 0;
-    RF_TRY(cuda_status(cudaGetDevice(&dev)));
-    if (dev < 0 || dev >= kMaxDevices) return RF_ERR_NOT_SUPPORTED;
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_scratch[dev]) {
-        void* p = nullptr;
-        RF_TRY(cuda_status(cudaGetSymbolAddress(&p, g_ghost_frft_scratch)));
-        g_static_scratch[dev] = (float*)p;
-    }
-    *out = g_static_scratch[dev];
+    void* p = nullptr;
+    RF_TRY(cuda_status(cudaGetSymbolAddress(&p, g_ghost_frft_scratch)));
+    *out = (float*)p;
     return RF_OK;
 }
 }  // namespace

@@ -13,7 +13,7 @@ from functools import lru_cache
 import numpy as np
 
 from . import glass
-from .constants import LAMBDA_MAX, LAMBDA_MIN, lens_element_dtype
+from .constants import LAMBDA_MAX, LAMBDA_MIN, RESOURCES, lens_element_dtype
 from .data import LensElement, LensModel, RealflareError, cast
 
 
@@ -29,11 +29,22 @@ def model_from_path(lens_model_path: str) -> LensModel:
         raise RealflareError(f'Invalid Lens Model: {lens_model_path}') from None
 
 
+def decode_path(path: str) -> str:
+    """``$RES`` names the bundled resources (the reference's ``storage.decode_path``,
+    ``realflare/storage.py:80,139-150``, maps it to its own resources directory); other
+    variables expand from the environment."""
+    normalized = path.replace('\\', '/')
+    if normalized == '$RES' or normalized.startswith('$RES/'):
+        path = os.path.join(RESOURCES, *normalized[len('$RES/'):].split('/'))
+    return os.path.expandvars(path)
+
+
 def resolve_model(lens) -> LensModel:
-    """The lens model of a ``Flare.Lens``: a model object or a JSON path."""
+    """The lens model of a ``Flare.Lens``: a model object or a JSON path (``$RES/model/...``
+    selects one of the bundled prescriptions)."""
     if lens.lens_model is not None:
         return lens.lens_model
-    return model_from_path(os.path.expandvars(lens.lens_model_path))
+    return model_from_path(decode_path(lens.lens_model_path))
 
 
 @lru_cache(16)

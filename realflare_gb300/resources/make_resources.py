@@ -11,8 +11,13 @@ The render path needs two public data tables at run time:
   own test relies on (``tests/glass.py:15-30`` expects BAFN6 first).
 * ``ciexyz.csv``: the CIE 2006 10-degree colour matching table of
   ``realflare/utils/ciexyz.py:4-406`` (wavelength nm, X, Y, Z).
+* ``model/<maker>/<name>.json``: the seven published lens prescriptions the reference
+  ships in ``realflare/resources/model`` (patent data), re-serialised unchanged, so that a
+  project's ``$RES/model/...`` lens path resolves here as it does in the reference
+  (``realflare/storage.py:80``).
 
-Usage: ``python realflare_gb300/resources/make_resources.py /path/to/reference``.
+Usage: ``python realflare_gb300/resources/make_resources.py <reference checkout>`` (or the
+checkout in the ``REALFLARE_REFERENCE`` environment variable).
 PyYAML is not needed: only the two fields above are read, line by line.
 """
 from __future__ import annotations
@@ -82,6 +87,25 @@ def make_cie_table(reference: str) -> list[list[float]]:
     raise ValueError('CIEXYZ table not found')
 
 
+def copy_lens_models(reference: str) -> list[str]:
+    source = os.path.join(reference, 'realflare', 'resources', 'model')
+    written = []
+    for maker in sorted(os.listdir(source)):
+        if not os.path.isdir(os.path.join(source, maker)):
+            continue
+        for file_name in sorted(os.listdir(os.path.join(source, maker))):
+            if not file_name.endswith('.json'):
+                continue
+            with open(os.path.join(source, maker, file_name), encoding='utf-8') as f:
+                data = json.load(f)
+            os.makedirs(os.path.join(HERE, 'model', maker), exist_ok=True)
+            with open(os.path.join(HERE, 'model', maker, file_name), 'w', encoding='utf-8') as f:
+                json.dump(data, f, indent=2)
+                f.write('\n')
+            written.append(f'{maker}/{file_name}')
+    return written
+
+
 def main(reference: str) -> None:
     glasses = make_glass_table(reference)
     with open(os.path.join(HERE, 'schott.json'), 'w', encoding='utf-8') as f:
@@ -91,8 +115,12 @@ def main(reference: str) -> None:
         f.write('# wavelength_nm,X,Y,Z (CIE 2006 10 degree)\n')
         for row in cie:
             f.write(','.join(repr(v) for v in row) + '\n')
-    print(f'{len(glasses)} glasses, {len(cie)} CIE rows')
+    models = copy_lens_models(reference)
+    print(f'{len(glasses)} glasses, {len(cie)} CIE rows, {len(models)} lens models')
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    checkout = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('REALFLARE_REFERENCE')
+    if not checkout:
+        sys.exit('usage: make_resources.py <reference checkout> (or set REALFLARE_REFERENCE)')
+    main(checkout)

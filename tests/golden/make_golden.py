@@ -59,15 +59,18 @@ def generate(name) -> dict:
 
 
 def main() -> None:
-    manifest = {}
+    manifest_path = os.path.join(HERE, 'manifest.json')
+    with open(manifest_path) as f:
+        manifest = json.load(f)  # other fixtures' entries (make_frft_golden.py) stay
     for name in CASES:
         arrays = generate(name)
         path = os.path.join(HERE, f'{name}.npz')
         np.savez_compressed(path, **arrays)
         manifest[name] = {k: hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest() for k, v in arrays.items()}
         print(name, {k: v.shape for k, v in arrays.items()}, os.path.getsize(path))
-    with open(os.path.join(HERE, 'manifest.json'), 'w') as f:
+    with open(manifest_path, 'w') as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
+        f.write('\n')
 
 
 if __name__ == '__main__':

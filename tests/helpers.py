@@ -56,3 +56,44 @@ def oracle_pipeline(o, w, ghost, spectrum):
     masks = o.bin_masks(bounds, ra.screen_transform, ra.width, ra.height, ra.bin_size)
     image = o.raster(vtx, masks, ghost, spectrum, ra)
     return dict(inputs=ti, rays=rays, bounds=bounds, inten=inten, vtx=vtx, masks=masks, image=image, raster_args=ra)
+
+
+def stratified_pixels(width: int, height: int, cells: int = 8, span: int = 16, seed: int = 0) -> np.ndarray:
+    """(n, 2) int32 x, y of cells x cells horizontal spans of ``span`` pixels, one span at a
+    seeded random place inside each cell of a cells x cells grid over the image."""
+    rng = np.random.default_rng(seed)
+    xy = []
+    for cy in range(cells):
+        for cx in range(cells):
+            y = int(rng.integers(cy * height // cells, (cy + 1) * height // cells))
+            x_lo, x_hi = cx * width // cells, max(cx * width // cells + 1, (cx + 1) * width // cells - span)
+            x0 = int(rng.integers(x_lo, x_hi))
+            xy += [(min(x0 + i, width - 1), y) for i in range(span)]
+    return np.unique(np.array(xy, np.int32), axis=0)
+
+
+def at_pixels(image: np.ndarray, xy: np.ndarray) -> np.ndarray:
+    """The RGBA values of the listed (unflipped x, y) pixels of a row-flipped image."""
+    return image[image.shape[0] - 1 - xy[:, 1], xy[:, 0]]
+
+
+def kept_paths(project, trace) -> tuple:
+    """The ghost paths PreprocessTask keeps (``preprocessing.py:22-103``: a 3 x 3 probe grid
+    over 1 % of the grid length, light at the centre, one wavelength; ghosts sorted by the
+    reference's ``x * x`` "area" of the first probe ray; the smallest kept), with ``trace``
+    (``Oracle.trace`` or ``Reference.trace`` with integer wavelengths) running the probe."""
+    import copy
+
+    from realflare_gb300.data import QPointF
+
+    q = copy.deepcopy(project)
+    q.render.grid_count, q.render.grid_length = 3, project.render.grid_length * 0.01
+    q.render.resolution, q.render.wavelength_count, q.render.wavelengths = QSize(100, 100), 1, ()
+    q.flare.light.position = QPointF(0, 0)
+    ti = prepare.trace_inputs(q)
+    rays = trace(ti.elements, ti.paths, ti.wavelengths.astype(np.int32), ti.args)
+    P = ti.args.path_count
+    x = rays[0].reshape(P, 1, 9)[:, 0, 0]
+    areas = {i: np.abs(x[i]) * np.abs(x[i]) for i in range(P)}
+    order = [k for k, _ in sorted(areas.items(), key=lambda item: item[1])]
+    return tuple(order[: int(P * (1 - project.render.cull_percentage))])

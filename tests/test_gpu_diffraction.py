@@ -122,6 +122,28 @@ def test_ghost_frft_matches_numpy(oracle, fstop):
     assert rel_l2(out.cpu().numpy(), ref) < 1e-4
 
 
+def test_ghost_frft_matches_reference_frft_fixture():
+    """rf_ghost_frft against ghost textures computed by the reference's own ``frft.py``
+    (``tests/golden/frft_ghost.npz``): every branch of ``frft.normalize``, square and
+    non-square apertures."""
+    import os
+
+    from golden.make_frft_golden import CASES, key
+
+    with np.load(os.path.join(os.path.dirname(__file__), 'golden', 'frft_ghost.npz')) as z:
+        g = {k: z[k] for k in z.files}
+    for case, h, w, _, _, fstops in CASES:
+        ap_d = torch.from_numpy(g[f'{case}_aperture']).cuda()
+        scratch = torch.empty((3, h, w, 2), device='cuda')
+        for fstop in fstops:
+            out = torch.empty((h, w), device='cuda')
+            alpha = 0.15 * (560.0 / 400) * (fstop / 18)
+            check(lib().rf_ghost_frft(ap_d.data_ptr(), w, h, alpha, scratch.data_ptr(), out.data_ptr(), stream()),
+                  'frft')
+            torch.cuda.synchronize()
+            assert rel_l2(out.cpu().numpy(), g[key(case, fstop)]) < 1e-4, (case, fstop)
+
+
 def starburst_args(w, h, sw, sh, samples=16, blur=0.01, rotation=0.2, weight=1.0, vig=(0.75, 1.0)):
     a = StarburstArgs()
     a.width, a.height, a.spectrum_width, a.spectrum_height, a.spectrum_count = w, h, sw, sh, 1
@@ -152,3 +174,50 @@ def test_starburst_matches_oracle(oracle):
     box = lambda a: a[..., :3].reshape(8, 8, 12, 8, 3).mean(axis=(1, 3))  # 8 x 8 pixel boxes
     assert rel_l2(box(got), box(ref)) < 3e-2
     assert abs(got[..., :3].sum() / ref[..., :3].sum() - 1) < 1e-2
+
+
+@pytest.mark.parametrize('vignetting', [(0.75, 1.0), (float('nan'), float('nan'))])
+def test_starburst_without_jitter_matches_oracle_tightly(oracle, vignetting):
+    """blur 0 and rotation 0 (the production settings): the jitter radius and the rotation
+    angle are exactly 0, so the noise hash no longer moves samples and the image is
+    deterministic up to FP32 rounding (``starburst.cl:1-87``)."""
+    from oracle.oracle import fft_power_spectrum
+
+    ap = aperture_image(oracle, 128)
+    spec = fft_power_spectrum(ap, 560e-6, 1000.0).astype(np.float32)
+    a = starburst_args(160, 96, 128, 128, samples=100, blur=0.0, rotation=0.0, vig=vignetting)
+    ref = oracle.starburst(spec, light_spectrum(), a)
+    img = torch.empty((96, 160, 4), device='cuda')
+    spec_d, light_d = torch.from_numpy(spec).cuda(), torch.from_numpy(light_spectrum()).cuda()
+    check(lib().rf_starburst(spec_d.data_ptr(), light_d.data_ptr(), ctypes.byref(a), img.data_ptr(), stream()),
+          'starburst')
+    torch.cuda.synchronize()
+    assert np.abs(ref[..., :3]).sum() > 0
+    assert rel_l2(img.cpu().numpy(), ref) < 1e-5
+
+
+def test_starburst_per_wavelength_spectra_match_oracle(oracle):
+    """One power spectrum per rendered wavelength (16 over 390-700 nm, each FFT'd with its own
+    wavelength; an extension of ``starburst.py:45-81``, which uses one at 560 nm): each
+    sample reads the spectrum of the nearest wavelength."""
+    from oracle.oracle import fft_power_spectrum
+
+    n = 64
+    ap = aperture_image(oracle, n)
+    wl = np.linspace(390.0, 700.0, 16)
+    spec = np.stack([fft_power_spectrum(ap, l * 1e-6, 1000.0) for l in wl]).astype(np.float32)
+    a = starburst_args(96, 64, n, n, samples=120, blur=0.0, rotation=0.0)
+    a.spectrum_count = len(wl)
+    a.lambda_first, a.lambda_step = float(wl[0]), float(wl[1] - wl[0])
+    ref = oracle.starburst(spec, light_spectrum(), a)
+    img = torch.empty((64, 96, 4), device='cuda')
+    spec_d, light_d = torch.from_numpy(spec).cuda(), torch.from_numpy(light_spectrum()).cuda()
+    check(lib().rf_starburst(spec_d.data_ptr(), light_d.data_ptr(), ctypes.byref(a), img.data_ptr(), stream()),
+          'starburst')
+    torch.cuda.synchronize()
+    # different from the single-spectrum image: the per-wavelength spectra are used
+    single = a
+    single.spectrum_count = 1
+    ref_single = oracle.starburst(spec[7], light_spectrum(), single)
+    assert rel_l2(ref, ref_single) > 1e-3
+    assert rel_l2(img.cpu().numpy(), ref) < 1e-5

@@ -3,7 +3,6 @@ construction, ghost paths, wavelengths, synthetic lenses and argument preparatio
 from __future__ import annotations
 
 import math
-import os
 
 import numpy as np
 import pytest
@@ -11,8 +10,6 @@ import pytest
 from realflare_gb300 import glass, lens, prepare, synthetic
 from realflare_gb300.constants import LAMBDA_MAX, LAMBDA_MIN, light_spectrum
 from realflare_gb300.data import Glass, LensElement, LensModel, Project, QSize, RealflareError, cast
-
-REFERENCE = os.environ.get('REALFLARE_REFERENCE', '/root/reference')
 
 
 def test_glass_catalogue_known_answers():
@@ -59,14 +56,18 @@ def test_ray_paths_and_wavelengths():
     assert light_spectrum().shape == (340, 4)
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, 'realflare')), reason='reference checkout absent')
 def test_real_lens_models_ghost_counts():
-    counts = {'Canon': 304, 'Kodak': 25, 'Leica': 36, 'Tronnier': 11, 'Zeiss': 127}
-    root = os.path.join(REFERENCE, 'realflare', 'resources', 'model')
-    for maker, n in counts.items():
-        d = os.path.join(root, maker)
-        f = os.path.join(d, sorted(os.listdir(d))[0])
-        assert len(lens.ray_paths(lens.model_from_path(f))) == n, maker
+    """The bundled prescriptions (the reference's ``realflare/resources/model``) resolve
+    through ``$RES`` and give the reference's ghost counts."""
+    counts = {'Canon/ef70-200mm-f2-8l-usm.json': 304, 'Kodak/100mm.json': 25, 'Leica/35mm_1_4.json': 36,
+              'Nikon/af_s_28_70mm.json': 157, 'Nikon/ai_50_135mm.json': 182, 'Tronnier/color-heliar.json': 11,
+              'Zeiss/zeiss-mp-50-t1-4.json': 127}
+    for name, n in counts.items():
+        model = lens.model_from_path(lens.decode_path(f'$RES/model/{name}'))
+        assert len(lens.ray_paths(model)) == n, name
+    p = Project()
+    p.flare.lens.lens_model_path = '$RES/model/Nikon/ai_50_135mm.json'
+    assert lens.resolve_model(p.flare.lens).aperture_index == 14
 
 
 def test_model_errors():

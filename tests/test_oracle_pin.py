@@ -63,6 +63,40 @@ def test_oracle_bit_identical_to_reference_kernels(pair, name):
     assert (ir_[..., :3] != 0).any()
 
 
+RASTER_MODES = [(1, 2), (1, 8), (2, 1), (4, 1), (4, 8), (8, 2)]
+
+
+@pytest.mark.parametrize('aa,ws', RASTER_MODES)
+@pytest.mark.parametrize('name', ['plain-8', 'spectral-16'])
+def test_oracle_raster_modes_bit_identical_to_reference_kernels(pair, name, aa, ws):
+    """Anti-aliasing (n-rook samples, ``rasterizing.cl:628-633``) and wavelength sub-steps
+    (``mix_vertex`` at ``wavelength_sub_pos`` with one spectrum lookup per step,
+    ``rasterizing.cl:606-650``): the oracle's image equals the reference kernels' bit for bit.
+    One wavelength (plain-8) turns the sub-steps off as ``rasterizing.py:390-392`` does."""
+    o, r = pair
+    kw = dict(grid=20, resolution=128) if name == 'plain-8' else dict(grid=16, resolution=128, paths=24,
+                                                                      wavelengths=4)
+    w = reduced(name, **kw)
+    w.project.flare.lens.coating_thickness = ()
+    w.project.render.anti_aliasing = aa
+    w.project.render.wavelength_sub_count = ws
+    ti = prepare.trace_inputs(w.project, w.paths)
+    a = ti.args
+    P, W, G = a.path_count, a.wavelength_count, a.grid_count
+    rays = r.trace(ti.elements, ti.paths, ti.wavelengths.astype(np.int32), a)
+    area, min_area = prepare.quad_constants(w.project)
+    bounds, inten = r.prim_shader(rays, P, W, G, area, min_area)
+    ghost = ghost_texture((48, 48), seed=3)
+    ra = prepare.raster_args(w.project, P, W, ghost.shape)
+    assert ra.sub_steps == aa and ra.wavelength_sub_count == (ws if W > 1 else 1)
+    vtx = r.vertex_shader(rays, inten, P, W, G, ra.screen_transform, ra.width, ra.height)
+    masks = r.binner(bounds, ra.screen_transform, ra.width, ra.height, ra.bin_size, local_size=64)
+    img_o = o.raster(vtx, masks, ghost, light_spectrum(), ra)
+    img_r = r.rasterizer(vtx, masks, ghost, light_spectrum(), ra)
+    assert np.array_equal(img_o, img_r)
+    assert (img_r[..., :3] != 0).any()
+
+
 def test_aperture_and_starburst_match_reference_kernels(pair):
     o, r = pair
     for blades, rot, rnd, soft in [(6, 0.0, 0.0, 0.0), (8, 0.4, 0.3, 0.03)]:

@@ -3,9 +3,10 @@
 Callers that cannot allocate device memory at render time (a plugin whose host
 application owns all device memory, a render loop that must not allocate after start-up)
 use this entry point; its scratch is a static device array shared by all calls. The test
-calls it through the C ABI twice in a row on different inputs and compares each result
-with rf_ghost_frft given a scratch buffer, and checks that sizes above the static
-maximum are refused. It runs last (file name) and also passes alone in a fresh process.
+calls it through the C ABI several times in a row on different inputs (among them the
+largest size, which fills the array to its end, a non-square one and the alpha branch that
+flips the spectrum) and compares each result with rf_ghost_frft given a scratch buffer,
+and checks that sizes above the static maximum are refused. It runs last (file name) and also passes alone in a fresh process.
 """
 from __future__ import annotations
 
@@ -24,30 +25,40 @@ from realflare_gb300._abi import RF_ERR_INVALID_ARG, RF_OK, lib  # noqa: E402
 RTOL = 1e-6
 
 
-def aperture(n, blades, rotation):
-    y, x = np.mgrid[-1:1:complex(0, n), -1:1:complex(0, n)]
+def aperture(h, w, blades, rotation):
+    y, x = np.mgrid[-1:1:complex(0, h), -1:1:complex(0, w)]
     angle = np.arctan2(y, x) + rotation
     r = np.hypot(x, y) * np.cos(np.pi / blades) / np.cos((angle % (2 * np.pi / blades)) - np.pi / blades)
     return (r < 0.75).astype(np.float32)
 
 
-def with_scratch(ap_d, n, alpha):
-    out = torch.empty((n, n), device='cuda')
-    scratch = torch.empty((3, n, n, 2), device='cuda')
+def with_scratch(ap_d, h, w, alpha):
+    out = torch.empty((h, w), device='cuda')
+    scratch = torch.empty((3, h, w, 2), device='cuda')
     s = int(torch.cuda.current_stream().cuda_stream)
-    assert lib().rf_ghost_frft(ap_d.data_ptr(), n, n, alpha, scratch.data_ptr(), out.data_ptr(), s) == RF_OK
+    assert lib().rf_ghost_frft(ap_d.data_ptr(), w, h, alpha, scratch.data_ptr(), out.data_ptr(), s) == RF_OK
     return out
+
+
+def alpha_of(fstop):
+    return 0.15 * (560 / 400) * (fstop / 18)
+
+
+# (height, width, blades, rotation, alpha): two ordinary calls in a row; the array filled to
+# its last element (512 x 512, and 64 x 4096 of the same pixel count, not square); alpha
+# 3.2, whose branch flips the spectrum into the third plane and copies it back
+CASES = [(256, 256, 6, 0.0, 0.0), (128, 128, 8, 0.3, alpha_of(40)), (512, 512, 8, 0.1, alpha_of(64)),
+         (64, 4096, 5, 0.2, alpha_of(8)), (128, 128, 6, 0.0, 3.2)]
 
 
 def test_static_scratch_matches_caller_scratch_on_two_calls():
     L = lib()
     s = int(torch.cuda.current_stream().cuda_stream)
-    cases = [(256, 6, 0.0, 0.0), (128, 8, 0.3, 0.15 * (560 / 400) * (40 / 18))]
-    for n, blades, rot, alpha in cases:
-        ap_d = torch.from_numpy(aperture(n, blades, rot)).cuda()
-        out = torch.empty((n, n), device='cuda')
-        assert L.rf_ghost_frft_static(ap_d.data_ptr(), n, n, alpha, out.data_ptr(), s) == RF_OK
-        ref = with_scratch(ap_d, n, alpha)
+    for h, w, blades, rot, alpha in CASES:
+        ap_d = torch.from_numpy(aperture(h, w, blades, rot)).cuda()
+        out = torch.empty((h, w), device='cuda')
+        assert L.rf_ghost_frft_static(ap_d.data_ptr(), w, h, alpha, out.data_ptr(), s) == RF_OK
+        ref = with_scratch(ap_d, h, w, alpha)
         torch.cuda.synchronize()
         got, want = out.cpu().numpy(), ref.cpu().numpy()
         assert np.isfinite(got).all() and np.linalg.norm(want) > 0
