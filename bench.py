@@ -45,6 +45,8 @@ def parse_args():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--workload', default=WORKLOAD)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--cpu-whole-frames', action='store_true',
+                    help='also measure a whole 16-surface CPU frame (about a minute) beside its sampled estimate')
     ap.add_argument('--no-e2e', action='store_true')
     # reductions of the workload for profiler captures (recorded in the line's config)
     ap.add_argument('--image', type=int, default=0, help='square image size override')
@@ -55,6 +57,8 @@ def parse_args():
                     help='skip the forward+adjoint measurement of the 16-surface lens')
     ap.add_argument('--no-diagram', action='store_true',
                     help='skip the DIAGRAM element measurement (trace with hits and drawing)')
+    ap.add_argument('--no-configs', action='store_true',
+                    help='skip the 8- and 16-surface FLARE frames measured beside the production frame')
     ap.add_argument('--raster-stats', action='store_true',
                     help='count k_raster work (statistics build of the library) instead of timing')
     ap.add_argument('--differentiable-only', action='store_true',
@@ -176,7 +180,7 @@ class GpuFrame:
 
     STAGES = ('ghost', 'trace', 'setup', 'bin', 'raster', 'starburst', 'compose')
 
-    def __init__(self, workload) -> None:
+    def __init__(self, workload, flare_only: bool = False) -> None:
         import numpy as np
         import torch
 
@@ -232,6 +236,7 @@ class GpuFrame:
         self.spectrum_tex = self.raster.spectrum()
         self.entries = 0
         self.events = None
+        self.flare_only = flare_only
 
     def _ev(self):
         e = self.torch.cuda.Event(enable_timing=True)
@@ -275,6 +280,10 @@ class GpuFrame:
                                   self.ghost.data_ptr(), self.spectrum_tex.data_ptr(), ctypes.byref(self.ra),
                                   self.flare.data_ptr(), s), 'raster')
         ev.append(self._ev())
+        if self.flare_only:  # a FLARE frame: no starburst, no composite
+            ev += [self._ev(), self._ev()]
+            self.events = ev
+            return
         # starburst: aperture (shape x blurred dust), spectrum, compositor
         sa = p.flare.starburst_aperture
         check(L.rf_aperture_shape(self.star_ap.data_ptr(), self.sw, self.sh_, sa.shape.size.width(),
@@ -314,20 +323,49 @@ class GpuFrame:
 
 
 # ---------------------------------------------------------------------- CPU baseline
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith('model name'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open('/proc/cpuinfo') as f:
+            for line in f:
+                if line.lower().startswith('model name'):
+                    return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return 'unknown'
+
+
 class CpuBaseline:
     """The reference's own kernels on the host cores (oracle/_ref, OpenMP over all cores;
     the C oracle when they are not built), timed on bounded samples of one frame.
 
     The whole frame's inputs (rays, primitives, vertices, bin masks, ghost texture,
-    starburst spectrum) are computed once on the host, untimed; ``measure()`` then times,
-    per stage: the trace, prim and vertex shaders of 2 ghosts and the binner on their
-    primitives (scaled by ghosts), the rasteriser on a stratified sample of pixels (a span
-    of SPAN pixels at the centre of each cell of a GRID x GRID grid over the image, scaled
-    by pixels), one starburst row (scaled by rows), and the numpy FFT stages whole.
+    starburst spectrum) are computed once on the host, untimed. ``measure(seed)`` then
+    times each stage on a sample and scales it to the whole frame:
+
+    * trace: every k-th ghost (about 12), scaled by surface interactions (loop steps
+      1 + elements + 2 (b1 - b2) per ray), since ghosts differ in length;
+    * prim and vertex shaders on those ghosts' rays and the binner on their primitives,
+      scaled by ghosts;
+    * rasteriser: 64 stratified spans of 16 pixels (one at a seeded place in each cell of
+      an 8 x 8 grid over the image), all in one parallel region, scaled by pixels;
+    * starburst: a band of 32 rows at a seeded height, one parallel region, scaled by rows;
+    * numpy FFT stages (starburst spectrum and ghost FRFT) whole.
+
+    Different seeds draw different samples; their spread bounds the extrapolation error.
     """
 
     SPAN = 16
-    GRID = 4
+    CELLS = 8
+    TRACE_GHOSTS = 12
+    STAR_ROWS = 32
 
     def __init__(self, workload) -> None:
         import numpy as np
@@ -338,12 +376,14 @@ class CpuBaseline:
 
         self.np = np
         self.orc = orc
+        self.prepare = prepare
         try:
             self.ref = orc.Reference()
             self.kind = 'reference'
         except (OSError, RuntimeError):
             self.ref, self.kind = None, 'port'
         self.o = orc.Oracle('f32')
+        self.cpu = self.ref if self.ref is not None else self.o
         p = workload.project
         self.p = p
         ti = prepare.trace_inputs(p)
@@ -356,12 +396,9 @@ class CpuBaseline:
         gr = p.render.ghost.resolution
         self.ra = prepare.raster_args(p, self.P, self.W, (gr.height(), gr.width()))
         self.spec = light_spectrum()
-        wl_int = ti.wavelengths.astype(np.int32)
+        self.threads = self.ref.set_threads(0) if self.ref is not None else os.cpu_count()
         # whole-frame inputs, untimed
-        if self.ref is not None:
-            rays = self.ref.trace(ti.elements, ti.paths, wl_int, a)
-        else:
-            rays = self.o.trace(ti.elements, ti.paths, ti.wavelengths, a)
+        rays = self.trace_rays(ti)
         bounds, inten = self.o.quad_setup(rays, self.P, self.W, self.G, self.area, self.min_area)
         ra = self.ra
         self.vtx = self.o.vertex(rays, inten, self.P, self.W, self.G, ra.screen_transform, ra.width, ra.height)
@@ -381,53 +418,18 @@ class CpuBaseline:
             noise = rng.random((sr.height(), sr.width()), dtype=np.float32)
             ap = self.o.aperture_noise_dust(ap, noise, sa.dust.strength, sa.dust.blur_sigma)
         self.star_ap = ap
+        self.fourier = orc.fft_power_spectrum(ap, 560e-6, max(1e-9, p.flare.starburst.distance * 1e3)).astype(
+            np.float32)
 
-    def measure(self) -> dict:
-        np, o, ref, ti = self.np, self.o, self.ref, self.ti
-        a, ra = ti.args, self.ra
-        P, W, G, R, Q = self.P, self.W, self.G, self.R, self.Q
-        out = {}
-        t0 = time.perf_counter()
-        if ref is not None:
-            ref.trace(ti.elements, ti.paths, ti.wavelengths.astype(np.int32), a, 0, 2 * W * R)
-        else:
-            o.trace(ti.elements, ti.paths, ti.wavelengths, a, 0, 2 * W * R)
-        out['trace'] = (time.perf_counter() - t0) * P / 2
-        from realflare_gb300 import prepare
+    def trace_rays(self, ti):
+        if self.ref is not None:
+            return self.ref.trace(ti.elements, ti.paths, ti.wavelengths.astype(self.np.int32), ti.args)
+        return self.o.trace(ti.elements, ti.paths, ti.wavelengths, ti.args)
 
-        a2 = prepare.trace_inputs(self.p, paths=ti.paths[:2]).args
-        rays2 = o.trace(ti.elements, ti.paths[:2], ti.wavelengths, a2)
-        t0 = time.perf_counter()
-        if ref is not None:
-            b2, i2 = ref.prim_shader(rays2, 2, W, G, self.area, self.min_area)
-            ref.vertex_shader(rays2, i2, 2, W, G, ra.screen_transform, ra.width, ra.height)
-            ref.binner(self.bounds[: 2 * Q], ra.screen_transform, ra.width, ra.height, ra.bin_size)
-        else:
-            b2, i2 = o.quad_setup(rays2, 2, W, G, self.area, self.min_area)
-            o.vertex(rays2, i2, 2, W, G, ra.screen_transform, ra.width, ra.height)
-            o.bin_masks(self.bounds[: 2 * Q], ra.screen_transform, ra.width, ra.height, ra.bin_size)
-        out['setup_bin'] = (time.perf_counter() - t0) * P / 2
-        h, w = ra.height, ra.width
-        t_r = 0.0
-        g = self.GRID
-        spans = [((2 * j + 1) * h // (2 * g), (2 * i + 1) * w // (2 * g) - self.SPAN // 2)
-                 for j in range(g) for i in range(g)]
-        for y, x in spans:
-            t0 = time.perf_counter()
-            if ref is not None:
-                ref.rasterizer(self.vtx, self.masks, self.ghost, self.spec, ra, rows=(y, y + 1),
-                               cols=(x, x + self.SPAN))
-            else:
-                o.raster(self.vtx, self.masks, self.ghost, self.spec, ra, rows=(y, y + 1), cols=(x, x + self.SPAN))
-            t_r += time.perf_counter() - t0
-        out['raster'] = t_r * (h * w) / (len(spans) * self.SPAN)
-        t0 = time.perf_counter()
-        f = self.orc.fft_power_spectrum(self.star_ap, 560e-6, max(1e-9, self.p.flare.starburst.distance * 1e3))
-        self.orc.ghost_texture(self.ghost_ap, self.p.flare.ghost.fstop, self.ghost_ap.shape)
-        out['fft'] = time.perf_counter() - t0
-        f = f.astype(np.float32)
+    def starburst_args(self, h, w):
         from realflare_gb300._abi import StarburstArgs
 
+        f = self.fourier
         sa = StarburstArgs()
         sa.width, sa.height = w, h
         sa.spectrum_width, sa.spectrum_height, sa.spectrum_count = f.shape[1], f.shape[0], 1
@@ -436,28 +438,143 @@ class CpuBaseline:
         sa.vignetting[0] = sa.vignetting[1] = float('nan')
         sa.intensity = 1e-6
         sa.scale[0], sa.scale[1] = 1.0, 1.0
+        sa.lambda_first, sa.lambda_step = 560.0, 1.0
+        return sa
+
+    def measure(self, seed: int = 0, small: bool = False) -> dict:
+        """Per-stage seconds of one whole frame, extrapolated from this seed's samples.
+        ``small`` shrinks every sample (for the one-thread figure)."""
+        np, cpu, ti, prepare = self.np, self.cpu, self.ti, self.prepare
+        ra = self.ra
+        P, W, G = self.P, self.W, self.G
+        out = {}
+        # trace and setup: every k-th ghost, starting at a seeded offset
+        n_ghosts = 2 if small else min(self.TRACE_GHOSTS, P)
+        step = max(1, P // n_ghosts)
+        sel = np.arange(seed % step, P, step)[:n_ghosts]
+        sub = prepare.trace_inputs(self.p, paths=ti.paths[sel])
         t0 = time.perf_counter()
-        if ref is not None:
-            ref.starburst(f, self.spec, sa, rows=(h // 2, h // 2 + 1))
+        rays = self.trace_rays(sub)
+        t_trace = time.perf_counter() - t0
+        out['trace'] = t_trace * trace_interactions(ti) / trace_interactions(sub)
+        k = len(sel)
+        t0 = time.perf_counter()
+        if self.ref is not None:
+            b, i = self.ref.prim_shader(rays, k, W, G, self.area, self.min_area)
+            self.ref.vertex_shader(rays, i, k, W, G, ra.screen_transform, ra.width, ra.height)
+            self.ref.binner(b, ra.screen_transform, ra.width, ra.height, ra.bin_size)
         else:
-            o.starburst(f, self.spec, sa, rows=(h // 2, h // 2 + 1))
-        out['starburst'] = (time.perf_counter() - t0) * h
+            b, i = self.o.quad_setup(rays, k, W, G, self.area, self.min_area)
+            self.o.vertex(rays, i, k, W, G, ra.screen_transform, ra.width, ra.height)
+            self.o.bin_masks(b, ra.screen_transform, ra.width, ra.height, ra.bin_size)
+        out['setup_bin'] = (time.perf_counter() - t0) * P / k
+        # raster: stratified spans in one parallel region
+        h, w = ra.height, ra.width
+        xy = self.orc.stratified_pixels(w, h, cells=self.CELLS, span=4 if small else self.SPAN, seed=seed)
+        image = np.zeros((h, w, 4), np.float32)
+        t0 = time.perf_counter()
+        if self.ref is not None:
+            self.ref.rasterizer_pixels(self.vtx, self.masks, self.ghost, self.spec, ra, xy, image)
+        else:
+            self.o.raster_pixels(self.vtx, self.masks, self.ghost, self.spec, ra, xy, image)
+        out['raster'] = (time.perf_counter() - t0) * (h * w) / len(xy)
+        # numpy FFT stages, whole
+        t0 = time.perf_counter()
+        self.orc.fft_power_spectrum(self.star_ap, 560e-6, max(1e-9, self.p.flare.starburst.distance * 1e3))
+        self.orc.ghost_texture(self.ghost_ap, self.p.flare.ghost.fstop, self.ghost_ap.shape)
+        out['fft'] = time.perf_counter() - t0
+        # starburst: a band of rows
+        rows = 1 if small else min(self.STAR_ROWS, h)
+        y0 = int(np.random.default_rng(seed).integers(0, h - rows + 1))
+        sa = self.starburst_args(h, w)
+        t0 = time.perf_counter()
+        cpu.starburst(self.fourier, self.spec, sa, rows=(y0, y0 + rows))
+        out['starburst'] = (time.perf_counter() - t0) * h / rows
         return out
 
-    def summary(self, stages: dict) -> dict:
-        total = sum(stages.values())
-        return {
-            'value': 1.0 / total,
+    def measure_one_thread(self) -> dict:
+        """measure(small=True) with one OpenMP thread (the reference kernels only)."""
+        if self.ref is None:
+            return None
+        previous = self.ref.set_threads(1)
+        try:
+            return self.measure(seed=0, small=True)
+        finally:
+            self.ref.set_threads(previous)
+
+    def summary(self, samples: list, one_thread: dict | None = None) -> dict:
+        """samples: per-seed stage seconds. value: frames/s of the median frame estimate."""
+        totals = sorted(sum(st.values()) for st in samples)
+        median = statistics.median(totals)
+        stages = {k: statistics.median(st[k] for st in samples) for k in samples[0]}
+        out = {
+            'value': 1.0 / median,
             'unit': 'frames/s',
-            'cores': os.cpu_count(),
+            'cores': self.threads,
+            'cpu_model': cpu_model(),
             'kind': self.kind,
-            'sample': (f'one frame of this workload: trace, prim/vertex shaders and binner on 2 of '
-                       f'{self.P} ghosts, rasteriser on {self.GRID * self.GRID} spans of {self.SPAN} pixels (one '
-                       f'per cell of a {self.GRID}x{self.GRID} grid), 1 starburst row, numpy FFT stages whole; '
-                       f'each stage scaled to the whole frame'),
+            'build': 'g++/gcc -O3 -fopenmp -ffp-contract=off (no -march=native: one source for x86 and Arm)',
+            'sample': (f'one frame of this workload per seed ({len(samples)} seeds): trace of every k-th ghost '
+                       f'({min(self.TRACE_GHOSTS, self.P)} of {self.P}) scaled by surface interactions, prim/vertex '
+                       f'shaders and binner on their primitives scaled by ghosts, rasteriser on '
+                       f'{self.CELLS * self.CELLS} stratified spans of {self.SPAN} pixels in one parallel region '
+                       f'scaled by pixels, starburst on {self.STAR_ROWS} rows, numpy FFT stages whole'),
             'stage_seconds': {k: round(v, 3) for k, v in stages.items()},
+            'frame_seconds_per_seed': [round(t, 2) for t in totals],
+            'spread': round((totals[-1] - totals[0]) / median, 4),
             'rays_per_s': self.n_rays / stages['trace'],
         }
+        if one_thread is not None:
+            t1 = sum(one_thread.values())
+            out['one_thread'] = {'value': 1.0 / t1, 'unit': 'frames/s', 'cores': 1,
+                                 'stage_seconds': {k: round(v, 2) for k, v in one_thread.items()},
+                                 'sample': '2 ghosts traced, 64 spans of 4 pixels, 1 starburst row'}
+        return out
+
+
+def whole_frame_check(name: str) -> dict:
+    """One whole frame of a flare-only workload (8-surface, or 16-surface) with the
+    reference's kernels on all host cores, stage by stage, beside the sampled estimate of
+    the same frame: the measured extrapolation error."""
+    import numpy as np
+
+    from oracle import oracle as orc
+    from realflare_gb300 import synthetic
+
+    w = synthetic.workload(name, integer_wavelengths=True)
+    base = CpuBaseline(w)
+    cpu, ra = base.cpu, base.ra
+    t0 = time.perf_counter()
+    rays = base.trace_rays(base.ti)
+    t_trace = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if base.ref is not None:
+        b, i = base.ref.prim_shader(rays, base.P, base.W, base.G, base.area, base.min_area)
+        v = base.ref.vertex_shader(rays, i, base.P, base.W, base.G, ra.screen_transform, ra.width, ra.height)
+        m = base.ref.binner(b, ra.screen_transform, ra.width, ra.height, ra.bin_size)
+    else:
+        b, i = base.o.quad_setup(rays, base.P, base.W, base.G, base.area, base.min_area)
+        v = base.o.vertex(rays, i, base.P, base.W, base.G, ra.screen_transform, ra.width, ra.height)
+        m = base.o.bin_masks(b, ra.screen_transform, ra.width, ra.height, ra.bin_size)
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if base.ref is not None:
+        base.ref.rasterizer(v, m, base.ghost, base.spec, ra)
+    else:
+        base.o.raster(v, m, base.ghost, base.spec, ra)
+    t_raster = time.perf_counter() - t0
+    whole = t_trace + t_setup + t_raster
+    est = [base.measure(seed) for seed in range(4)]
+    est_flare = [e['trace'] + e['setup_bin'] + e['raster'] for e in est]
+    return {
+        'workload': name, 'kind': base.kind, 'cores': base.threads,
+        'rays': base.n_rays, 'image': f'{ra.width}x{ra.height}',
+        'measured_seconds': {'trace': round(t_trace, 3), 'setup_bin': round(t_setup, 3),
+                             'raster': round(t_raster, 3), 'flare': round(whole, 3)},
+        'measured_frames_per_s': 1.0 / whole, 'measured_rays_per_s': base.n_rays / t_trace,
+        'sampled_flare_seconds': [round(x, 3) for x in est_flare],
+        'sampled_over_measured': round(statistics.median(est_flare) / whole, 4),
+    }
 
 
 # ---------------------------------------------------------------------- main
@@ -492,25 +609,28 @@ def trace_interactions(ti) -> int:
 
 
 def run_reference(args, rank, world) -> None:
+    """The reference arm: each step is one frame estimate from a seeded sample (the seeds
+    differ between steps) of the reference's kernels on all host cores."""
     if rank != 0:
         return
     w = make_workload(args)
     cpu = CpuBaseline(w)
-    stages, times = None, []
+    samples, times = [], []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        st = cpu.measure()
+        st = cpu.measure(seed=i)
         if i >= args.warmup:
             times.append(time.perf_counter() - t0)
-            stages = st
-    s = cpu.summary(stages)
+            samples.append(st)
+    s = cpu.summary(samples)
     line = {
         'impl': 'reference', 'metric': METRIC,
         'value': s['value'], 'unit': 'frames/s', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': 1e3 / s['value'], 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32', 'data': 'synthetic',
         'config': workload_config(w, args.gpus),
-        'cpu_baseline': {k: s[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
+        'cpu_baseline': {k: s[k] for k in ('value', 'unit', 'cores', 'kind', 'sample', 'cpu_model', 'build',
+                                           'spread', 'frame_seconds_per_seed')},
         'e2e': {'value': s['value'], 'unit': 'frames/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'stage_seconds': s['stage_seconds'], 'rays_per_s': s['rays_per_s'],
         'sample_wall_s': statistics.median(times) if times else None,
@@ -568,6 +688,7 @@ def main() -> None:
     batched = run_batched(args) if args.batched_frames > 0 and rank == 0 else None
     differentiable = run_differentiable(args) if not args.no_differentiable and rank == 0 else None
     diagram = run_diagram(args) if not args.no_diagram and rank == 0 else None
+    configs = run_configs(args) if not args.no_configs and rank == 0 else None
 
     peak, peak_kind = load_peaks()
     raster_s = last['raster'] / 1e3
@@ -599,18 +720,20 @@ def main() -> None:
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         base = CpuBaseline(w)
-        s = base.summary(base.measure())
-        cpu = {k: s[k] for k in ('value', 'unit', 'cores', 'kind', 'sample', 'stage_seconds', 'rays_per_s')}
+        cpu = base.summary([base.measure(seed) for seed in range(4)], base.measure_one_thread())
+        del base
+        cpu['whole_frame_check'] = [whole_frame_check('plain-8')]
+        if args.cpu_whole_frames:
+            cpu['whole_frame_check'].append(whole_frame_check('spectral-16'))
     if rank == 0:
         line = {
             'metric': METRIC,
             'value': fps, 'unit': 'frames/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': dict(workload_config(w, world), **{
-                'l2': f'per-frame working set (rays {frame.rays.numel() * 4 / 1e9:.2f} GB, tile entries '
-                      f'{entries * 4 / 1e9:.2f} GB) > L2 (129 MB): no flush needed',
-            }),
+            'config': workload_config(w, world),
+            'l2': (f'per-frame working set (rays {frame.rays.numel() * 4 / 1e9:.2f} GB, tile entries '
+                   f'{entries * 4 / 1e9:.2f} GB) > L2 (129 MB): inputs larger than L2, no flush'),
             'rays_per_s': frame.n_rays / (last['trace'] / 1e3) * world,
             # k_trace: FP32 / issue-bound (no DRAM or tensor bound applies)
             'trace': {
@@ -631,12 +754,49 @@ def main() -> None:
             'batched': batched,
             'differentiable': differentiable,
             'diagram': diagram,
+            'configs': configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_configs(args, steps: int = 20) -> dict:
+    """FLARE frames (ghost texture, trace, setup, binning, raster; no starburst) of the
+    8-surface workload (512^2, 28 ghosts, 32^2 grid, 1 wavelength) and the 16-surface
+    workload (1024^2, 120 ghosts, 64^2 grid, 8 wavelengths) with device-resident inputs:
+    frames/s and rays/s (CUDA events over ``steps`` frames after 3 warm-up frames)."""
+    import torch
+
+    from realflare_gb300 import synthetic
+
+    out = {}
+    for name in ('plain-8', 'spectral-16'):
+        frame = GpuFrame(synthetic.workload(name), flare_only=True)
+        for _ in range(3):
+            frame.step()
+        torch.cuda.synchronize()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(frame.stream)
+        trace_ms = []
+        for _ in range(steps):
+            frame.step()
+            trace_ms.append(frame.events)
+        stop.record(frame.stream)
+        torch.cuda.synchronize()
+        seconds = start.elapsed_time(stop) / 1e3 / steps
+        t_trace = statistics.median(ev[1].elapsed_time(ev[2]) for ev in trace_ms) / 1e3
+        stage = frame.stage_ms()
+        out[name] = {
+            'image': f'{frame.ra.width}x{frame.ra.height}', 'ghosts': frame.P, 'wavelengths': frame.W,
+            'grid': frame.G, 'rays': frame.n_rays, 'frames_per_s': 1.0 / seconds, 'ms_per_frame': seconds * 1e3,
+            'rays_per_s': frame.n_rays / t_trace,
+            'stage_ms': {k: round(v, 4) for k, v in stage.items() if k not in ('starburst', 'compose')},
+        }
+        del frame
+    return out
 
 
 def run_raster_stats(args) -> None:

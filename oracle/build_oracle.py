@@ -30,7 +30,7 @@ def build(force: bool = False) -> None:
         if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
             continue
         cmd = [
-            'gcc', '-O2', '-std=gnu11', '-fopenmp', '-fPIC', '-shared', '-ffp-contract=off',
+            'gcc', '-O3', '-std=gnu11', '-fopenmp', '-fPIC', '-shared', '-ffp-contract=off',
             f'-DRFO_REAL={real}', SRC, '-o', out + '.tmp', '-lm',
         ]
         procs.append((subprocess.Popen(cmd), out))

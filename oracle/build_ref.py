@@ -118,7 +118,7 @@ def build(reference: str | None = None, force: bool = False) -> str | None:
     objs, procs = [], []
     for src in sources:
         obj = src[:-4] + '.o'
-        cmd = ['g++', '-O2', '-std=gnu++17', '-fopenmp', '-fPIC', '-ffp-contract=off', '-w',
+        cmd = ['g++', '-O3', '-std=gnu++17', '-fopenmp', '-fPIC', '-ffp-contract=off', '-w',
                '-c', src, '-o', obj]
         procs.append(subprocess.Popen(cmd))
         objs.append(obj)

@@ -384,6 +384,21 @@ def ghost_texture(aperture: np.ndarray, fstop: float, resolution: tuple) -> np.n
     return np.abs(spectrum) * np.sqrt(resolution[0] * resolution[1])
 
 
+def stratified_pixels(width: int, height: int, cells: int = 8, span: int = 16, seed: int = 0) -> np.ndarray:
+    """(n, 2) int32 x, y of cells x cells horizontal spans of ``span`` pixels, one span at a
+    seeded random place inside each cell of a cells x cells grid over the image (the pixel
+    samples of the parity tests and of the timed CPU baseline)."""
+    rng = np.random.default_rng(seed)
+    xy = []
+    for cy in range(cells):
+        for cx in range(cells):
+            y = int(rng.integers(cy * height // cells, (cy + 1) * height // cells))
+            x_lo, x_hi = cx * width // cells, max(cx * width // cells + 1, (cx + 1) * width // cells - span)
+            x0 = int(rng.integers(x_lo, x_hi))
+            xy += [(min(x0 + i, width - 1), y) for i in range(span)]
+    return np.unique(np.array(xy, np.int32), axis=0)
+
+
 def reference_available() -> bool:
     return Reference.available()
 

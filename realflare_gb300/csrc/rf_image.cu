@@ -79,13 +79,16 @@ __global__ void __launch_bounds__(256) k_starburst(const float* __restrict__ spe
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int t = t0 + i;
             const float step = (float)t / (float)a.samples;
-            const float wavelength = step * (float)(RF_LAMBDA_MAX - RF_LAMBDA_MIN) + (float)RF_LAMBDA_MIN;
+            // no contraction into an FMA: the spectrum index below rounds this value, and a
+            // sample can fall exactly halfway between two spectra
+            const float wavelength = __fadd_rn(__fmul_rn(step, (float)(RF_LAMBDA_MAX - RF_LAMBDA_MIN)),
+                                               (float)RF_LAMBDA_MIN);
             StarburstSample e;
             // chromatic scale 1 - (1 - lambda / 560) (LAMBDA_MID is an int in starburst.cl)
             e.scale = fmaxf(1.0f - (1.0f - (wavelength / (float)RF_LAMBDA_MID)) * 1.0f, 1.17549435e-38f);
             int sidx = 0;
             if (a.spectrum_count > 1) {
-                const int k = cvt_rz_sat(floorf((wavelength - a.lambda_first) / a.lambda_step + 0.5f));
+                const int k = cvt_rz_sat(floorf(__fadd_rn(__fsub_rn(wavelength, a.lambda_first) / a.lambda_step, 0.5f)));
                 sidx = k < 0 ? 0 : (k >= a.spectrum_count ? a.spectrum_count - 1 : k);
             }
             e.sidx = sidx;

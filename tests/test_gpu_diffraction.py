@@ -199,7 +199,9 @@ def test_starburst_without_jitter_matches_oracle_tightly(oracle, vignetting):
 def test_starburst_per_wavelength_spectra_match_oracle(oracle):
     """One power spectrum per rendered wavelength (16 over 390-700 nm, each FFT'd with its own
     wavelength; an extension of ``starburst.py:45-81``, which uses one at 560 nm): each
-    sample reads the spectrum of the nearest wavelength."""
+    sample reads the spectrum of the nearest wavelength. With 120 samples, sample 62 lies
+    exactly halfway between spectra 8 and 9 (17 * 62 / 124 = 8.5): the tie is rounded up
+    in both implementations."""
     from oracle.oracle import fft_power_spectrum
 
     n = 64
