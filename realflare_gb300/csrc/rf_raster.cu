@@ -182,20 +182,24 @@ __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float
         d[i] = sx[i] * sx[j] + sy[i] * sy[j];
         r2[i] = sx[i] * sx[i] + sy[i] * sy[i];
     }
-    // a_i are integers (differences of products of integers), so their product is 0 exactly
-    // when one of them is 0, and otherwise at least 1 and finite; a vertex on the sample
-    // point (r2_i = 0, s_i = 0) makes a_i and a_{i-1} exactly 0, so it is rare too
-    const bool rare = (a[0] * a[1]) * (a[2] * a[3]) == 0.0f;
+    // The common case first. a_i are integers (differences of products of integers): when
+    // none is 0 each |a_i| >= 1 and every term below is finite, so the weight sum is finite.
+    // An a_i of 0 makes t_i infinite or NaN, and a vertex on the sample point (r2_i = 0)
+    // makes r_i NaN; either way the sum is not finite, and only then are the weights redone
+    // with the reference's special cases (the rare path).
+    static_assert(!RF_RASTER_EXACT_SMALL_ANGLES, "the rare path is entered only for a_i == 0 or r_i == 0");
     float ir[4], r[4], t[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         ir[i] = rsqrtf(r2[i]);
         r[i] = r2[i] * ir[i];
     }
-    if (!rare) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) t[i] = (r[i] * r[(i + 1) & 3] - d[i]) * __fdividef(1.0f, a[i]);
-    } else {
+    for (int i = 0; i < 4; i++) t[i] = (r[i] * r[(i + 1) & 3] - d[i]) * __fdividef(1.0f, a[i]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) * ir[i];
+    float sum = w[0] + w[1] + w[2] + w[3];
+    if (!(fabsf(sum) <= 3.40282347e38f)) {
         bool zero = false;
 #pragma unroll
         for (int i = 0; i < 4; i++) zero = zero || r2[i] == 0.0f;
@@ -220,10 +224,11 @@ __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float
                 t[i] = (r[i] * r[j] - d[i]) * __fdividef(1.0f, a[i]);
             }
         }
-    }
 #pragma unroll
-    for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) * ir[i];
-    const float inv = __fdividef(1.0f, w[0] + w[1] + w[2] + w[3]);
+        for (int i = 0; i < 4; i++) w[i] = (t[(i + 3) & 3] + t[i]) * ir[i];
+        sum = w[0] + w[1] + w[2] + w[3];
+    }
+    const float inv = __fdividef(1.0f, sum);
 #pragma unroll
     for (int i = 0; i < 4; i++) w[i] *= inv;
 }
@@ -231,7 +236,7 @@ __device__ __forceinline__ void barycentric_fast(const Rec& rec, float px, float
 // Bilinear ghost sample (read_imagef LINEAR, CLAMP -> border 0, rasterizing.cl:483-485)
 // at texel coordinates (u, v) = uv * size - 0.5.
 __device__ __forceinline__ float ghost_sample(const float* __restrict__ tex, int w, int h, float u, float v) {
-    if (!(fabsf(u) < 1e9f) || !(fabsf(v) < 1e9f)) return 0.0f;  // non-finite or far outside
+    if (!(fabsf(u) + fabsf(v) < 2e9f)) return 0.0f;  // non-finite or far outside
     const float fu = floorf(u), fv = floorf(v);
     const float a = u - fu, b = v - fv;
     const int i0 = (int)fu, j0 = (int)fv;
