@@ -317,6 +317,25 @@ class GpuFrame:
         ev.append(self._ev())
         self.events = ev
 
+    def accurate_trace_ms(self, reps: int = 3) -> float:
+        """Milliseconds of rf_trace_accurate (double-precision ray geometry) on this frame's
+        inputs, into the same ray buffer (CUDA events on the frame's stream, after one
+        untimed run)."""
+        from realflare_gb300._abi import check
+
+        def run():
+            check(self.lib.rf_trace_accurate(self.elements.data_ptr(), self.paths.data_ptr(),
+                                             self.wavelengths.data_ptr(), ctypes.byref(self.ti.args),
+                                             self.rays.data_ptr(), self.sh), 'rf_trace_accurate')
+
+        run()
+        start, stop = self._ev(), None
+        for _ in range(reps):
+            run()
+        stop = self._ev()
+        stop.synchronize()
+        return start.elapsed_time(stop) / reps
+
     def stage_ms(self) -> dict:
         ev = self.events
         return {name: ev[i].elapsed_time(ev[i + 1]) for i, name in enumerate(self.STAGES)}
@@ -681,6 +700,7 @@ def main() -> None:
     elapsed = max_over_ranks(elapsed, world)
     fps = args.steps / elapsed * world
 
+    trace_accurate_ms = frame.accurate_trace_ms() if rank == 0 else None
     # e2e through the Engine API: host Project in, host image out
     e2e = None
     if not args.no_e2e:
@@ -741,8 +761,12 @@ def main() -> None:
                 'surface_interactions': interactions,
                 'surface_interactions_per_s': interactions / (last['trace'] / 1e3) * world,
                 'issue_active': trace_prof.get('issue_active_small'),
+                'accurate_ms': trace_accurate_ms,
+                'accurate_frame_ms': (elapsed / args.steps * 1e3 - last['trace'] + trace_accurate_ms
+                                      if trace_accurate_ms else None),
                 'note': ('interactions: 1 + elements + 2 (b1 - b2) loop steps per ray that reaches the sensor; '
-                         'issue_active: ncu smsp__issue_active of k_trace, 1024^2 / 48-ghost case'),
+                         'issue_active: ncu smsp__issue_active of k_trace, 1024^2 / 48-ghost case; accurate_ms: '
+                         'rf_trace_accurate (double-precision ray geometry) on the same frame'),
             },
             'stage_ms': {k: round(v, 3) for k, v in last.items()},
             'tile_entries': entries,

@@ -100,6 +100,18 @@ long long rf_launch_count(void);
 int rf_trace(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
              const rf_trace_args* args, float* rays, void* stream);
 
+/* rf_trace with the ray geometry in double precision (an opt-in accurate mode; the same
+ * kernel of realflare/api/tasks/cl/raytracing.cl:218-359, the same arguments and layout).
+ * Grid point, light direction, intersect (raytracing.cl:123-175), refract and reflect
+ * (70-102), dispersion (107-120), aperture position and rrel are evaluated in double and
+ * rounded to float on output; the coating and Fresnel reflectances (1-59) are FP32. The
+ * reference's FP32 positions (rf_trace) differ from the same trace in double by a few ulps,
+ * which the rasteriser's integer sample coordinates can turn into whole-pixel changes; this
+ * mode's positions are those of the double evaluation. Several times slower than rf_trace
+ * (double-precision throughput). */
+int rf_trace_accurate(const rf_lens_element* elements, const int32_t* paths, const float* wavelengths,
+                      const rf_trace_args* args, float* rays, void* stream);
+
 /* One surface hit of a traced ray (the reference's Intersection, realflare/api/tasks/
  * opencl.py:18-25, without the float3 padding): position and unit normal at the surface,
  * the incidence angle acos(-dir . normal) (0 on flat elements), hit 1 (0 in an unused

@@ -145,6 +145,7 @@ F32 = ctypes.c_float
 # name -> argtypes (every entry point returns int status)
 SIGNATURES = {
     'rf_trace': [P, P, P, ctypes.POINTER(TraceArgs), P, P],
+    'rf_trace_accurate': [P, P, P, ctypes.POINTER(TraceArgs), P, P],
     'rf_trace_intersections': [P, P, P, ctypes.POINTER(TraceArgs), P, P, I32, P],
     'rf_diagram': [P, I32, I32, F32, P, I32, I32, I32, I32, P, P],
     'rf_quad_setup': [P, I32, I32, I32, F32, F32, P, P, P],

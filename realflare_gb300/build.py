@@ -28,6 +28,8 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 UNITS = {
     'rf_api.cu': [],
     'rf_trace.cu': ['-ftz=true'] + ([] if os.environ.get('RF_TRACE_FMAD') == '1' else ['-fmad=false']),
+    # the accurate trace's double arithmetic is the oracle's double build operation for operation
+    'rf_trace_accurate.cu': ['-ftz=true', '-fmad=false'],
     'rf_quad.cu': ['-fmad=false'],
     'rf_sort.cu': [],
     'rf_bin.cu': [],

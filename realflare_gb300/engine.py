@@ -23,8 +23,13 @@ logger = logging.getLogger(__name__)
 
 
 class Engine:
-    def __init__(self, device: str = '', cache: bool = True) -> None:
+    """``accurate_trace=True`` selects the double-precision ray geometry of
+    ``RaytracingTask(accurate=True)`` for the single-light flares this engine renders
+    (image-based lights render through the batched path, whose trace is FP32)."""
+
+    def __init__(self, device: str = '', cache: bool = True, accurate_trace: bool = False) -> None:
         self.cache = cache
+        self.accurate_trace = accurate_trace
         self.queue = None
         self.image: Image | None = None
         self._device = device
@@ -37,7 +42,7 @@ class Engine:
         self.starburst_aperture_task = tasks.StarburstApertureTask(self.queue)
         self.ghost_task = tasks.GhostTask(self.queue)
         self.starburst_task = tasks.StarburstTask(self.queue)
-        self.raytracing_task = tasks.RaytracingTask(self.queue, cache=self.cache)
+        self.raytracing_task = tasks.RaytracingTask(self.queue, cache=self.cache, accurate=self.accurate_trace)
         self.rasterizing_task = tasks.RasterizingTask(self.queue)
         self.preprocess_task = tasks.PreprocessTask(self.queue)
         self.image_sampling_task = tasks.ImageSamplingTask(self.queue)

@@ -49,19 +49,24 @@ class Task:
 
 
 class RaytracingTask(Task):
-    """Spectral trace of every ghost path (``realflare/api/tasks/raytracing.py:37-247``)."""
+    """Spectral trace of every ghost path (``realflare/api/tasks/raytracing.py:37-247``).
 
-    def __init__(self, queue=None, cache: bool = True) -> None:
+    ``accurate=True`` traces the ray geometry in double precision (``rf_trace_accurate``):
+    positions equal the double evaluation of the reference's trace rounded to float, instead
+    of the reference's FP32 values, at the cost of double-precision throughput."""
+
+    def __init__(self, queue=None, cache: bool = True, accurate: bool = False) -> None:
         super().__init__(queue)
         self._cache = None
         self.use_cache = cache
+        self.accurate = accurate
 
     def raytrace(self, project: Project, path_indexes: tuple = (), paths=None) -> Rays | None:
         inputs = prepare.trace_inputs(project, paths=paths, path_indexes=path_indexes)
         if inputs is None:
             return None
         key = (inputs.elements.tobytes(), inputs.paths.tobytes(), inputs.wavelengths.tobytes(),
-               bytes(inputs.args))
+               bytes(inputs.args), self.accurate)
         if self.use_cache and self._cache is not None and self._cache[0] == key:
             return self._cache[1]
         a = inputs.args
@@ -70,8 +75,9 @@ class RaytracingTask(Task):
         wl = to_device(inputs.wavelengths)
         rays = empty((6, inputs.ray_count))
         if inputs.ray_count:
-            check(self.lib.rf_trace(ptr(elements), ptr(paths_t), ptr(wl), ctypes.byref(a), ptr(rays), self.stream),
-                  'rf_trace')
+            trace = self.lib.rf_trace_accurate if self.accurate else self.lib.rf_trace
+            check(trace(ptr(elements), ptr(paths_t), ptr(wl), ctypes.byref(a), ptr(rays), self.stream),
+                  'rf_trace_accurate' if self.accurate else 'rf_trace')
         shape = (a.path_count, a.wavelength_count, a.grid_count**2)
         result = Rays(rays, shape, args=key)
         result.inputs = inputs
