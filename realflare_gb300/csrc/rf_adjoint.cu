@@ -5,11 +5,14 @@
 // rrel, reflectance), rf_trace_adjoint returns the gradient with respect to every lens
 // element's radius, center and coating thicknesses and to the (normalised) light direction.
 //
-// Per ray, the thread re-traces the ray with the forward's own code (rf_trace_core.cuh,
-// compiled like rf_trace.cu without floating-point contraction, so the re-trace takes the
-// same path), recording the position and direction entering each element; the surfaces
-// (hit point, normal) are recomputed from those in the reverse sweep instead of being
-// stored. The reverse sweep applies, element by element from the sensor back to the entry,
+// Per ray, the thread re-traces the ray from its entry with the forward's own code
+// (rf_trace_core.cuh, compiled like rf_trace.cu without floating-point contraction, so the
+// re-trace takes the same path). It keeps only every kCheckpoint-th step's state (position
+// and direction entering the element) and one byte per step (element, reflected or not);
+// the reverse sweep goes back one segment of kCheckpoint steps at a time, re-tracing the
+// segment from its checkpoint with the same step code to regenerate the states entering its
+// elements, and recomputes each surface hit (point, normal) from them: no bounce is stored.
+// The reverse sweep applies, element by element from the sensor back to the entry,
 // the transposed Jacobians of intersect (sphere or plane), refract, reflect and the coating
 // reflectance (the last by three-tangent forward-mode duals of the Fresnel formulas), then
 // the entry ray (grid point hitting element 0, stepped back along the light direction).
@@ -30,6 +33,13 @@ constexpr int kAdjThreads = 128;
 #endif
 constexpr int kAdjMaxElements = 32;
 constexpr int kAdjMaxSteps = 3 * kAdjMaxElements;
+// steps between stored states (segments re-traced in the reverse sweep)
+#ifndef RF_ADJOINT_CHECKPOINT
+#define RF_ADJOINT_CHECKPOINT 8
+#endif
+constexpr int kCheckpoint = RF_ADJOINT_CHECKPOINT;
+constexpr int kMaxCheckpoints = (kAdjMaxSteps + kCheckpoint - 1) / kCheckpoint;
+static_assert(kAdjMaxElements <= 128, "an element index and the reflection flag share one byte");
 constexpr int kAdjTableRows = 4;
 constexpr int kGradPerElement = 4;  // radius, center, coating thickness 0 and 1
 
@@ -126,17 +136,21 @@ __device__ __noinline__ D3 fresnel_two_layer_d(D3 theta0, float lambda, float n0
 }
 
 // ---------------------------------------------------------------- recording
-struct Step {
+// The state entering a loop step: position and direction.
+struct State {
     float px, py, pz, dx, dy, dz;
-    int tag;  // element index | 1 << 16 when the ray reflects at this element
 };
-struct StepRecorder {
-    Step* steps;
+struct CheckpointRecorder {
+    State* checkpoints;  // the state entering steps 0, kCheckpoint, 2 kCheckpoint, ...
+    unsigned char* tags;  // per step: element index | 0x80 when the ray reflects there
     int n;
     int argmax;  // step whose |xy| / height is the final rrel
     float best;
     __device__ __forceinline__ void step(int lens, float px, float py, float pz, float dx, float dy, float dz) {
-        if (n < kAdjMaxSteps) steps[n] = {px, py, pz, dx, dy, dz, lens};
+        if (n < kAdjMaxSteps) {
+            if (n % kCheckpoint == 0) checkpoints[n / kCheckpoint] = {px, py, pz, dx, dy, dz};
+            tags[n] = (unsigned char)lens;
+        }
         n++;
     }
     __device__ __forceinline__ void hit(int, const Hit&, float, float, float, bool) {}
@@ -147,7 +161,7 @@ struct StepRecorder {
         }
     }
     __device__ __forceinline__ void reflect() {
-        if (n - 1 < kAdjMaxSteps) steps[n - 1].tag |= 1 << 16;
+        if (n - 1 < kAdjMaxSteps) tags[n - 1] |= 0x80;
     }
 };
 
@@ -304,8 +318,9 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
             needed = needed || g_out[k] != 0.0f;
         }
     }
-    Step steps[kAdjMaxSteps];
-    StepRecorder rec{steps, 0, -1, 0.0f};
+    State checkpoints[kMaxCheckpoints];
+    unsigned char tags[kAdjMaxSteps];
+    CheckpointRecorder rec{checkpoints, tags, 0, -1, 0.0f};
     float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (needed)
         trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
@@ -320,12 +335,42 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
     const float refl = out[5];
     V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);  // adjoint of the state leaving a step
     bool apt_pending = true;  // the last aperture crossing sets pos_apt
+    // the states entering the steps of the current segment, regenerated from its checkpoint
+    // by the forward's step (intersect, then reflect or refract; the stop and the sensor
+    // keep the direction)
+    State seg[kCheckpoint];
     for (int j = n_steps - 1; j >= 0; j--) {
+        if (j == n_steps - 1 || (j + 1) % kCheckpoint == 0) {
+            const int j0 = j - j % kCheckpoint;
+            if (valid && j0 < rec.n) {
+                State st = checkpoints[j0 / kCheckpoint];
+                const int j1 = min(j + 1, rec.n);
+                for (int q = j0; q < j1; q++) {
+                    seg[q - j0] = st;
+                    if (q + 1 == j1) break;
+                    const int i = tags[q] & 0x7f;
+                    const Hit h = intersect(st.px, st.py, st.pz, st.dx, st.dy, st.dz, se[i]);
+                    const State in = st;
+                    st.px = h.px;
+                    st.py = h.py;
+                    st.pz = h.pz;
+                    if (i == p.aperture || i == E - 1) continue;
+                    const int n_index = (in.dz < 0.0f) ? i - 1 : i + 1;
+                    if (tags[q] & 0x80) {
+                        reflect_dir(st.dx, st.dy, st.dz, h);
+                    } else {
+                        const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
+                        refract_dir(st.dx, st.dy, st.dz, h, n1, ior_of(i));
+                    }
+                }
+            }
+        }
         float g4[kGradPerElement] = {0.f, 0.f, 0.f, 0.f};
         int el = 0;
         if (valid && j < rec.n) {
-            const Step& st = steps[j];
-            const int i = st.tag & 0xffff;
+            const State& st = seg[j % kCheckpoint];
+            const int tag = tags[j];
+            const int i = tag & 0x7f;
             el = i;
             const SmemElement& e = se[i];
             const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
@@ -357,7 +402,7 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
                     const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
                     const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
                     const float n2 = ior_of(i);
-                    if (st.tag >> 16) {
+                    if (tag & 0x80) {
                         // d' = d - 2 (d.n) n
                         const float dn = dot(din, nrm), gdn = dot(gd, nrm);
                         gdin = gd - nrm * (2.0f * gdn);

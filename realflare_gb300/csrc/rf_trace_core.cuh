@@ -161,6 +161,27 @@ __device__ __forceinline__ float dispersion(float lambda, const float* c) {
     return sqrtf(1.0f + d0 + d1 + d2);
 }
 
+// reflect (raytracing.cl:96-102): d + n * 2 (n . -d)
+__device__ __forceinline__ void reflect_dir(float& dx, float& dy, float& dz, const Hit& h) {
+    float k = 2.0f * (h.nx * -dx + h.ny * -dy + h.nz * -dz);
+    dx = dx + h.nx * k;
+    dy = dy + h.ny * k;
+    dz = dz + h.nz * k;
+}
+
+// refract (raytracing.cl:70-86) with o = n1 / n2; the direction is zeroed past total
+// internal reflection
+__device__ __forceinline__ void refract_dir(float& dx, float& dy, float& dz, const Hit& h, float n1, float n2) {
+    const float o = n1 / n2;
+    const float cost = -dx * h.nx + -dy * h.ny + -dz * h.nz;
+    const float sint2 = (o * o) * (1.0f - cost * cost);
+    const float k = o * cost - sqrtf(fabsf(1.0f - sint2));
+    const float valid = (float)(sint2 < 1.0f);
+    dx = (o * dx + k * h.nx) * valid;
+    dy = (o * dy + k * h.ny) * valid;
+    dz = (o * dz + k * h.nz) * valid;
+}
+
 // Per-frame constants of the trace.
 struct TraceFrame {
     int E, aperture, W, G, R;
@@ -241,11 +262,7 @@ __device__ __forceinline__ void trace_ray_rec(const SmemElement* __restrict__ se
         if (do_reflect) {
             rec.reflect();
             const float incident = incident_angle(dx, dy, dz, h);
-            // reflect, raytracing.cl:96-102
-            float k = 2.0f * (h.nx * -dx + h.ny * -dy + h.nz * -dz);
-            dx = dx + h.nx * k;
-            dy = dy + h.ny * k;
-            dz = dz + h.nz * k;
+            reflect_dir(dx, dy, dz, h);
             // theta = incident + 1e-9 (a double sum there); only angles below 0.02 rad
             // are close enough to 1e-9 for the double sum to differ from `incident`
             float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
@@ -261,15 +278,7 @@ __device__ __forceinline__ void trace_ray_rec(const SmemElement* __restrict__ se
             }
             if (reflectance > 0.0f) refl *= reflectance;
         } else {
-            // refract, raytracing.cl:70-86
-            const float o = n1 / n2;
-            const float cost = -dx * h.nx + -dy * h.ny + -dz * h.nz;
-            const float sint2 = (o * o) * (1.0f - cost * cost);
-            const float k = o * cost - sqrtf(fabsf(1.0f - sint2));
-            const float valid = (float)(sint2 < 1.0f);
-            dx = (o * dx + k * h.nx) * valid;
-            dy = (o * dy + k * h.ny) * valid;
-            dz = (o * dz + k * h.nz) * valid;
+            refract_dir(dx, dy, dz, h, n1, n2);
             if (dz == 0.0f) break;
         }
     }
