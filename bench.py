@@ -627,6 +627,95 @@ def trace_interactions(ti) -> int:
     return int(per_ray.sum()) * ti.args.wavelength_count * ti.args.grid_count ** 2
 
 
+# FP32 operations of the reference's trace arithmetic (realflare/api/tasks/cl/raytracing.cl,
+# as written: no fused multiply-adds; add, subtract, multiply, divide, square root and each
+# sin/cos/tan/asin/acos call count 1; comparisons, min/max, abs and negation 0). The
+# refractive index of a (wavelength, element) is one value per frame, so dispersion is not
+# counted per interaction.
+TRACE_FLOPS = {
+    'intersect_sphere': 59,   # intersect 123-175 with the incidence acos (sphere)
+    'intersect_flat': 8,      # intersect, flat element
+    'aperture': 2,            # pos_apt = pos.xy / height
+    'rrel': 5,                # max(rrel, length(pos.xy) / height)
+    'refract': 26,            # n1 / n2 and refract 70-86
+    'reflect': 14,            # reflect 96-102, theta = incident + 1e-9, reflectance *= R
+    'fresnel': 24,            # fresnel 1-16 (uncoated)
+    'fresnel_ar': 77,         # nc, d1 and fresnel_ar 18-59 (single layer)
+    'two_layer': 149,         # the exact two-layer stack (no reference counterpart)
+    'init': 20,               # grid point, normalize(-direction), back-off (plus the intersect)
+}
+# One fragment of the rasteriser (covered pixel x record): compute_barycentric_quad
+# (rasterizing.cl:95-148) 67, fragment_shader (471-506) times the hits 71, the colour lookup
+# and accumulation (640-650) 12, counted the same way.
+RASTER_FRAGMENT_FLOPS = 150
+# The same fragment as the fewest instructions (multiply-adds fused, reciprocal, rsqrt and
+# floor one each, the record's per-corner terms set up once per record): mean-value weights
+# 68, fragment 49 (four of them the texel loads).
+RASTER_FRAGMENT_MIN_INSTRUCTIONS = 117
+
+
+def trace_flops(ti) -> int:
+    """FP32 operations of a whole trace, every ray completing its path (TRACE_FLOPS per loop
+    step, walking each ghost path's element sequence by the reference's loop rules,
+    raytracing.cl:258-352)."""
+    el = ti.elements
+    E, apt = ti.args.element_count, ti.args.aperture_index
+    R = ti.args.grid_count ** 2
+    f = TRACE_FLOPS
+    total = 0
+    for b1, b2 in ti.paths.astype(int):
+        ops = f['init'] + (f['intersect_sphere'] if el['radius'][0] != 0 else f['intersect_flat'])
+        step, delta, i = 0, 1, 0
+        while 0 <= i < E:
+            ops += f['intersect_sphere'] if el['radius'][i] != 0 else f['intersect_flat']
+            if i == apt:
+                ops += f['aperture']
+            else:
+                ops += f['rrel']
+                if i != E - 1:
+                    if (step == 0 and i == b1) or (step == 1 and i == b2):
+                        step += 1
+                        delta = -delta
+                        ops += f['reflect']
+                        if el['coating_layers'][i] == 2:
+                            ops += f['two_layer']
+                        elif el['coating_layers'][i] == 1 or el['coating'][i] > 0:
+                            ops += f['fresnel_ar']
+                        else:
+                            ops += f['fresnel']
+                    else:
+                        ops += f['refract']
+            i += delta
+        total += ops
+    return total * ti.args.wavelength_count * R
+
+
+def fp32_peak_tflops() -> float:
+    """Derived FP32 peak: SMs x 128 FP32 lanes x 2 (multiply-add) x the measured maximum SM
+    clock of this pool (MEASURED_PEAKS.json sm_max_mhz, else 2070 MHz)."""
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            mhz = float(json.load(fh).get('sm_max_mhz', mhz))
+    except (OSError, ValueError):
+        pass
+    sms = 152
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def issue_peak_ginstr() -> float:
+    """Instruction issue peak in thread instructions per second (G): SMs x 4 schedulers x 32
+    lanes x the maximum SM clock (one warp instruction per scheduler per cycle)."""
+    return fp32_peak_tflops() * 1e3 / 2.0
+
+
 def run_reference(args, rank, world) -> None:
     """The reference arm: each step is one frame estimate from a seeded sample (the seeds
     differ between steps) of the reference's kernels on all host cores."""
@@ -719,6 +808,7 @@ def main() -> None:
     prof = raster_profile()
     trace_prof = raster_profile('k_trace')
     interactions = trace_interactions(frame.ti)
+    flops = trace_flops(frame.ti)
     traffic = fragments = None
     if prof.get('workload') == args.workload and prof.get('tile_entries') == entries:
         # the summary was taken on this very launch (same workload, same tile entries)
@@ -732,6 +822,25 @@ def main() -> None:
         'fragments_per_s': fragments / raster_s if fragments else None,
         # the bound that limits this kernel: instruction issue (ncu on the reduced case)
         'issue_active': prof.get('issue_active_small'),
+        'issue': {
+            'bound': 'issue', 'unit': 'G thread-instructions/s',
+            'achieved': fragments * RASTER_FRAGMENT_MIN_INSTRUCTIONS / raster_s / 1e9 if fragments else None,
+            'peak': issue_peak_ginstr(),
+            'frac': (fragments * RASTER_FRAGMENT_MIN_INSTRUCTIONS / raster_s / 1e9 / issue_peak_ginstr()
+                     if fragments else None),
+            'instructions_per_fragment': RASTER_FRAGMENT_MIN_INSTRUCTIONS,
+            'note': ('the fewest instructions of one fragment of the reference arithmetic (multiply-adds fused) x '
+                     'fragments / time, against one warp instruction per scheduler per cycle at the maximum '
+                     'clock (derived)'),
+        },
+        'fp32': {
+            'bound': 'fp32', 'unit': 'TFLOP/s',
+            'achieved': fragments * RASTER_FRAGMENT_FLOPS / raster_s / 1e12 if fragments else None,
+            'peak': fp32_peak_tflops(),
+            'frac': fragments * RASTER_FRAGMENT_FLOPS / raster_s / 1e12 / fp32_peak_tflops() if fragments else None,
+            'flops_per_fragment': RASTER_FRAGMENT_FLOPS,
+            'note': 'FP32 peak derived: SMs x 128 lanes x 2 x maximum SM clock (none is measured in MEASURED_PEAKS.json)',
+        },
         'note': ('issue-bound per-fragment shading (mean-value weights, bilinear ghost lookup per covered '
                  'pixel x record): issue_active is the fraction of cycles the warp schedulers issue an '
                  'instruction (ncu smsp__issue_active, 1024^2 / 48-ghost case of the same kernel); the vertex '
@@ -761,6 +870,11 @@ def main() -> None:
                 'surface_interactions': interactions,
                 'surface_interactions_per_s': interactions / (last['trace'] / 1e3) * world,
                 'issue_active': trace_prof.get('issue_active_small'),
+                'flops': flops,
+                'flops_per_interaction': flops / interactions,
+                'fp32_tflops': flops / (last['trace'] / 1e3) / 1e12 * world,
+                'fp32_peak_tflops': fp32_peak_tflops(),
+                'fp32_frac': flops / (last['trace'] / 1e3) / 1e12 / fp32_peak_tflops(),
                 'accurate_ms': trace_accurate_ms,
                 'accurate_frame_ms': (elapsed / args.steps * 1e3 - last['trace'] + trace_accurate_ms
                                       if trace_accurate_ms else None),

@@ -148,9 +148,15 @@ class LensParameters:
 
 class DifferentiableRenderer:
     """The flare of one project (lens, ghosts, wavelengths, grid, image) as a differentiable
-    function of ``LensParameters``. ``render(params)`` returns the (h, w, 4) image tensor."""
+    function of ``LensParameters``. ``render(params)`` returns the (h, w, 4) image tensor.
 
-    def __init__(self, project: Project, ghost: torch.Tensor, paths=None, stream=None) -> None:
+    ``accurate=True`` runs the forward trace with the double-precision ray geometry
+    (``rf_trace_accurate``): the image, its coverage and the vertex attributes the gradient
+    is taken at are then those of the double evaluation of the trace, not the reference's
+    FP32 values (the adjoint's re-trace stays FP32: it only evaluates the Jacobians)."""
+
+    def __init__(self, project: Project, ghost: torch.Tensor, paths=None, stream=None,
+                 accurate: bool = False) -> None:
         from .tasks import RasterizingTask
 
         require_cuda()
@@ -178,6 +184,7 @@ class DifferentiableRenderer:
         self.task = RasterizingTask(self.stream)
         self.rays = empty((6, max(self.n_rays, 1)))
         self.params = LensParameters(project, dev)
+        self.accurate = accurate
 
     # -- kernels --------------------------------------------------------------------
     def _element_buffer(self, radius, center, thickness) -> torch.Tensor:
@@ -198,8 +205,9 @@ class DifferentiableRenderer:
         s = int(self.stream.cuda_stream)
         self.el = self._element_buffer(radius, center, thickness)
         self.targs = self._trace_args(direction)
-        check(self.lib.rf_trace(self.el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(),
-                                ctypes.byref(self.targs), self.rays.data_ptr(), s), 'rf_trace')
+        trace = self.lib.rf_trace_accurate if self.accurate else self.lib.rf_trace
+        check(trace(self.el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(),
+                    ctypes.byref(self.targs), self.rays.data_ptr(), s), 'rf_trace')
         from .device import Rays
 
         rays = Rays(self.rays, (self.P, self.W, self.G ** 2))
@@ -237,10 +245,152 @@ class DifferentiableRenderer:
         self.grad_rays = g_rays
         return g_el[:, 0], g_el[:, 1], g_el[:, 2], g_dir
 
+    def trace_kernels(self, radius, center, thickness, direction):
+        """The trace alone: (rays (6, n): positions, aperture positions, rrel, reflectance;
+        the element buffer and trace arguments, which its adjoint needs)."""
+        s = int(self.stream.cuda_stream)
+        el = self._element_buffer(radius, center, thickness)
+        targs = self._trace_args(direction)
+        rays = empty((6, max(self.n_rays, 1)))
+        trace = self.lib.rf_trace_accurate if self.accurate else self.lib.rf_trace
+        check(trace(el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(), ctypes.byref(targs),
+                    rays.data_ptr(), s), 'rf_trace')
+        return rays, el, targs
+
+    def trace_backward(self, el, targs, grad_rays: torch.Tensor):
+        """rf_trace_adjoint of a trace: (grad radius, center, thickness, normalised direction)."""
+        s = int(self.stream.cuda_stream)
+        g = grad_rays.to(torch.float32).contiguous()
+        g_el = empty((self.E, 4))
+        g_dir = empty((3,))
+        check(self.lib.rf_trace_adjoint(el.data_ptr(), self.paths.data_ptr(), self.wavelengths.data_ptr(),
+                                        ctypes.byref(targs), g.data_ptr(), g_el.data_ptr(), g_dir.data_ptr(), s),
+              'rf_trace_adjoint')
+        return g_el[:, 0], g_el[:, 1], g_el[:, 2], g_dir
+
     # -- torch ----------------------------------------------------------------------
     def render(self, radii, gaps, thickness, light) -> torch.Tensor:
         radius, center, t, direction = self.params.elements(radii, gaps, thickness, light, self.E)
         return FlareFunction.apply(radius, center, t, direction, self)
+
+    def trace(self, radii, gaps, thickness, light) -> torch.Tensor:
+        """The traced rays (6, n) as a differentiable function of the parameters."""
+        radius, center, t, direction = self.params.elements(radii, gaps, thickness, light, self.E)
+        return TraceFunction.apply(radius, center, t, direction, self)
+
+    def splat(self, rays: torch.Tensor, sigma: float, channels: bool = False) -> torch.Tensor:
+        """A smooth stand-in for the flare's energy distribution (the coarse stage of the
+        recovery): every traced ray's energy at its sensor position, splatted bilinearly
+        into the image and blurred by a Gaussian of ``sigma`` pixels.
+
+        The flare gives each quad the energy area_orig x the mean of its corners' ghost
+        texture, housing falloff and coating reflectance (fragment_shader with the 1 / area
+        intensity, rasterizing.cl:471-506); so a ray's weight here is that product (ghost
+        texture at the aperture position, smoothstep(1, 0.95, rrel), reflectance) times its
+        wavelength's colour, and the blurred splat approximates the blurred flare wherever the
+        blur is wider than the quads. Unlike the flare, it is smooth in the ray positions.
+        Returns (h, w) with the AP1 channels summed, or with ``channels`` the three channels
+        (3, h, w); row 0 at the top like the flare image."""
+        import torch.nn.functional as F
+
+        ra = self.raster_args
+        h, w = ra.height, ra.width
+        P, W, R = self.P, self.W, self.G ** 2
+        x = rays[0] * ra.screen_transform + w / 2  # vertex_shader's pixel mapping
+        y = rays[1] * ra.screen_transform + h / 2
+        valid = torch.isfinite(rays[5])
+        gs = ra.ghost_scale
+        grid = torch.stack([rays[2] / gs, rays[3] / gs], -1).view(1, 1, -1, 2)
+        gi = F.grid_sample(self.ghost.view(1, 1, *self.ghost.shape[:2]), torch.nan_to_num(grid), mode='bilinear',
+                           padding_mode='zeros', align_corners=False).view(-1)
+        t = ((rays[4] - 1.0) / (0.95 - 1.0)).clamp(0.0, 1.0)
+        ri = t * t * (3.0 - 2.0 * t)
+        refl = torch.nan_to_num(rays[5]).clamp_min(0.0)
+        colour = self._colour_weights()  # (W, 3)
+        colour = colour if channels else colour.sum(1, keepdim=True)
+        nc = colour.shape[1]
+        colour = colour.t().reshape(nc, 1, W, 1).expand(nc, P, W, R).reshape(nc, -1)
+        wgt = torch.where(valid, gi * ri * refl, torch.zeros_like(refl))[None] * colour  # (nc, n)
+        xs, ys = torch.nan_to_num(x) - 0.5, torch.nan_to_num(y) - 0.5
+        x0, y0 = torch.floor(xs), torch.floor(ys)
+        fx, fy = xs - x0, ys - y0
+        img = torch.zeros(nc, h * w, device=rays.device, dtype=rays.dtype)
+        for dx, dy, k in ((0, 0, (1 - fx) * (1 - fy)), (1, 0, fx * (1 - fy)), (0, 1, (1 - fx) * fy), (1, 1, fx * fy)):
+            xi, yi = x0.long() + dx, y0.long() + dy
+            inside = valid & (xi >= 0) & (xi < w) & (yi >= 0) & (yi < h)
+            idx = torch.where(inside, (h - 1 - yi) * w + xi, torch.zeros_like(xi))
+            img = img.index_add(1, idx, torch.where(inside, k, torch.zeros_like(k))[None] * wgt)
+        img = img.view(nc, h, w)
+        if not channels:
+            return gaussian_blur(img[0], sigma)
+        return torch.stack([gaussian_blur(img[c], sigma) for c in range(nc)])
+
+    def _colour_weights(self) -> torch.Tensor:
+        """Per wavelength, the AP1 colour its records get (W, 3): the spectrum texel at
+        position (w + 0.5) / W (rasterizing.cl:617-645, nearest texel); the last wavelength
+        only ends the last pair and weighs 0; one wavelength adds the fragment to every XYZ
+        channel (rasterizing.cl:648-650)."""
+        cache = self.__dict__.get('_colour')
+        if cache is None:
+            from .constants import light_spectrum
+
+            W = self.W
+            spec = light_spectrum().astype(np.float64)[:, :3]
+            c = np.zeros((W, 3))
+            for k in range(max(W - 1, 1)):
+                xyz = spec[min(int((k + 0.5) / W * spec.shape[0]), spec.shape[0] - 1)] if W > 1 else np.ones(3)
+                c[k] = XYZ_TO_AP1 @ xyz
+            cache = torch.tensor(c, dtype=torch.float32, device=self.base_elements.device)
+            self._colour = cache
+        return cache
+
+
+# color.cl:3-10
+XYZ_TO_AP1 = np.array([[1.6410233797, -0.3248032942, -0.2364246952],
+                       [-0.6636628587, 1.6153315917, 0.0167563477],
+                       [0.0117218943, -0.0082844420, 0.9883948585]])
+
+
+def gaussian_blur(img: torch.Tensor, sigma: float) -> torch.Tensor:
+    """Separable Gaussian blur (zero outside the image) of an (h, w) tensor."""
+    import torch.nn.functional as F
+
+    r = max(1, int(3 * sigma))
+    k = torch.exp(-0.5 * (torch.arange(-r, r + 1, device=img.device, dtype=img.dtype) / sigma) ** 2)
+    k = k / k.sum()
+    x = F.conv2d(img[None, None], k.view(1, 1, 1, -1), padding=(0, r))
+    x = F.conv2d(x, k.view(1, 1, -1, 1), padding=(r, 0))
+    return x[0, 0]
+
+
+def _direction_backward(direction: torch.Tensor, g_n: torch.Tensor) -> torch.Tensor:
+    """n = normalize(-v), v = direction: dn/dv = -(I - n n^T) / |v|."""
+    v = direction.to(torch.float64)
+    norm = torch.linalg.norm(v)
+    n = -v / norm
+    g_n = g_n.to(torch.float64)
+    return (-(g_n - n * torch.dot(n, g_n)) / norm).to(direction.dtype)
+
+
+class TraceFunction(torch.autograd.Function):
+    """rays = trace(radius, center, coating thickness per element, light direction.xyz); each
+    call keeps its own element buffer and trace arguments for its adjoint, so several traces
+    (other light positions) can precede one backward."""
+
+    @staticmethod
+    def forward(ctx, radius, center, thickness, direction, renderer: DifferentiableRenderer):
+        ctx.renderer = renderer
+        ctx.save_for_backward(direction)
+        with torch.no_grad():
+            rays, ctx.el, ctx.targs = renderer.trace_kernels(radius, center, thickness, direction)
+        return rays
+
+    @staticmethod
+    def backward(ctx, grad_rays):
+        (direction,) = ctx.saved_tensors
+        g_radius, g_center, g_thick, g_n = ctx.renderer.trace_backward(ctx.el, ctx.targs, grad_rays)
+        dt = direction.dtype
+        return (g_radius.to(dt), g_center.to(dt), g_thick.to(dt), _direction_backward(direction, g_n), None)
 
 
 class FlareFunction(torch.autograd.Function):
