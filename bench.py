@@ -1097,9 +1097,14 @@ def run_differentiable(args) -> dict:
         'workload': 'differentiable-16', 'image': '512x512', 'rays': r.n_rays,
         'parameters': sum(q.numel() for q in params),
         'forward_ms': f_ms, 'forward_adjoint_ms': fa_ms, 'ratio': fa_ms / f_ms,
-        'recovery': {'steps': rec.steps, 'loss_start': rec.loss_start, 'loss_end': rec.loss_end,
-                     'param_rms_error_start': rec.error_start, 'param_rms_error_end': rec.error_end,
-                     'seconds': rec.seconds},
+        'recovery': {'coarse_steps': rec.coarse_steps, 'image_steps': rec.steps,
+                     'loss_initial': rec.loss_initial, 'loss_before_image_stage': rec.loss_start,
+                     'loss_end': rec.loss_end, 'param_rms_error_start': rec.error_start,
+                     'param_rms_error_after_coarse': rec.error_after_coarse, 'param_rms_error_end': rec.error_end,
+                     'group_rms_error_start': rec.error_groups_start, 'group_rms_error_end': rec.error_groups_end,
+                     'seconds': rec.seconds,
+                     'stages': ('coarse: blurred ray splat against the blurred target (blur 8, 4, 2, 1 px); image: '
+                                '200 Adam steps of the image loss over the coating thicknesses')},
         'timing': 'wall clock per iteration (each includes the binning host synchronisation)',
     }
 
