@@ -25,11 +25,12 @@ namespace rf {
 namespace {
 
 constexpr int kAdjThreads = 128;
-// resident blocks per SM requested from the register allocator (6: 80 registers; the
-// per-ray step record already lives in local memory, and the few spills cost less than the
-// extra resident warps gain)
+// resident blocks per SM requested from the register allocator (8: 64 registers; the
+// checkpoints and the segment's states live in local memory, and the spills cost less than
+// the extra resident warps gain: 1.46 ms against 1.52 ms at 6 blocks and 1.67 ms at 4 on the
+// 16-surface differentiable workload)
 #ifndef RF_ADJOINT_MIN_BLOCKS
-#define RF_ADJOINT_MIN_BLOCKS 6
+#define RF_ADJOINT_MIN_BLOCKS 8
 #endif
 constexpr int kAdjMaxElements = 32;
 constexpr int kAdjMaxSteps = 3 * kAdjMaxElements;

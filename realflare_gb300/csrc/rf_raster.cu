@@ -773,11 +773,17 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     constexpr int kBlocks = T * T / 32, kCols = T / 8;
     extern __shared__ float4 smem4[];
     Rec* recbuf = (Rec*)smem4;  // two batches of records
+    // Where each record's gradients go: the vertex index of corner 0 at the pair's first
+    // wavelength and the sub-step's blend weight, set when the record is built and read by the
+    // batch's flush. Three batches' worth: the build of batch t + 2 may run while slower warps
+    // still flush batch t, and the build of t + 3 comes after the barrier of t + 1.
+    long long* vbase_buf = (long long*)(recbuf + 2 * kBatchRecords);  // [3][kBatchRecords]
+    float* tbuf = (float*)(vbase_buf + 3 * kBatchRecords);            // [3][kBatchRecords]
     // per-warp transpose buffers of each lane's 5 attribute gradients and 4 corner weights:
     // [row][lane], rows kRedStride floats apart (16-byte aligned, and the rows that lanes read
     // side by side fall in different bank groups)
-    float* red = (float*)(recbuf + 2 * kBatchRecords) + (threadIdx.x >> 5) * (kRedRows * kRedStride);
-    float* xyz = (float*)(recbuf + 2 * kBatchRecords) + 8 * kRedRows * kRedStride;
+    float* red = (tbuf + 3 * kBatchRecords) + (threadIdx.x >> 5) * (kRedRows * kRedStride);
+    float* xyz = (tbuf + 3 * kBatchRecords) + 8 * kRedRows * kRedStride;
     float* blend = xyz + 3 * p.maxW * p.WS;
     float* grgb = blend + ((p.WS + 3) & ~3);          // [block * 3 + channel][lane]: dL / d(linear XYZ sum)
     float* rgrad_buf = grgb + 96 * kBlocks;            // two batches of [record][corner * 5 + attribute]
@@ -839,13 +845,24 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     // warp), then one thread per record finishes it. Batches are double-buffered: warps that
     // are done shading batch t build batch t + 1 while the others shade, one barrier per
     // batch, and each batch sums its records' gradients in its own buffer.
-    auto build = [&](Rec* dst, uint32_t first) {
+    auto build = [&](Rec* dst, uint32_t first, int slot) {
         for (int h = 0; h < (kBatchRecords + 63) / 64; h++) {
             const int e = my_entry + 64 * h;
             if (e < per_batch && first + e < end) {
+                const uint32_t entry = tile_entries[first + e];
                 CornerLoad c;
-                load_corner(vtx, tile_entries[first + e], my_corner, p, c);
+                load_corner(vtx, entry, my_corner, p, c);
                 for (int i = 0; i < p.WS; i++) store_corner(c, my_corner, blend[i], S, fc, dst[e * p.WS + i]);
+                if (my_corner == 0) {  // where the record's gradients go (the batch's flush)
+                    const long long prim = entry / p.maxW;
+                    const int w = (int)(entry % p.maxW);
+                    const int quad = (int)(prim % Q);
+                    const long long v0 = ((prim / Q) * VC + (quad / (p.G - 1)) * p.G + quad % (p.G - 1)) * p.W + w;
+                    for (int i = 0; i < p.WS; i++) {
+                        vbase_buf[slot * kBatchRecords + e * p.WS + i] = v0;
+                        tbuf[slot * kBatchRecords + e * p.WS + i] = blend[i];
+                    }
+                }
             }
         }
         __syncwarp();  // the four corners of each record are stored
@@ -862,10 +879,10 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
         next_block[1] = 0;
     }
     __syncthreads();  // blend weights, colours and pixel gradients are set
-    if (begin < end) build(recbuf, begin);
+    if (begin < end) build(recbuf, begin, 0);
     __syncthreads();
-    int cur = 0;
-    for (uint32_t base = begin; base < end; base += per_batch, cur ^= 1) {
+    int cur = 0, slot = 0;  // record buffer (batch parity) and flush slot (batch index mod 3)
+    for (uint32_t base = begin; base < end; base += per_batch, cur ^= 1, slot = slot == 2 ? 0 : slot + 1) {
         const int n_rec = (int)min((uint32_t)per_batch, end - base) * p.WS;
         const Rec* recs = recbuf + cur * kBatchRecords;
         float* rgrad = rgrad_buf + cur * (kBatchRecords * 4 * kGradAttrs);
@@ -983,7 +1000,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                 }
             }
         }
-        if (base + per_batch < end) build(recbuf + (cur ^ 1) * kBatchRecords, base + per_batch);
+        if (base + per_batch < end) build(recbuf + (cur ^ 1) * kBatchRecords, base + per_batch, slot == 2 ? 0 : slot + 1);
         // the other counter was last used by the previous batch, behind the last barrier
         if (threadIdx.x == 0) next_block[cur ^ 1] = 0;
         __syncthreads();  // every block of this batch is shaded and the next batch is built
@@ -996,15 +1013,9 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
             rgrad[idx] = 0.0f;
             const int j = idx / (4 * kGradAttrs), rem = idx % (4 * kGradAttrs);
             const int corner = rem / kGradAttrs, a = rem % kGradAttrs;
-            const uint32_t entry = tile_entries[base + j / p.WS];
-            const float t = blend[j % p.WS];
-            const long long prim = entry / p.maxW;
-            const int w = (int)(entry % p.maxW);
-            const long long path = prim / Q;
-            const int quad = (int)(prim % Q);
-            const int c0 = (quad / (p.G - 1)) * p.G + quad % (p.G - 1);
-            const int cv = corner == 0 ? c0 : (corner == 1 ? c0 + 1 : (corner == 2 ? c0 + 1 + p.G : c0 + p.G));
-            const long long vi = (path * VC + cv) * p.W + w;
+            const float t = tbuf[slot * kBatchRecords + j];
+            const int offset = corner == 0 ? 0 : (corner == 1 ? 1 : (corner == 2 ? 1 + p.G : p.G));
+            const long long vi = vbase_buf[slot * kBatchRecords + j] + (long long)offset * p.W;
             atomicAdd(grad_vtx + 8 * vi + kGradSlot[a], g * (1.0f - t));
             atomicAdd(grad_vtx + 8 * (vi + 1) + kGradSlot[a], g * t);
         }
@@ -1288,7 +1299,8 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     p.T = T;
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
-    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
+    const size_t smem = sizeof(Rec) * 2 * kBatchRecords + (sizeof(long long) + sizeof(float)) * 3 * kBatchRecords +
+                        sizeof(float) * (3 * p.maxW * p.WS + ((p.WS + 3) & ~3)) +
                         sizeof(float) * (96 * (T * T / 32) + 2 * kBatchRecords * 4 * kGradAttrs +
                                          8 * kRedRows * kRedStride);
     const FragmentConsts fc = fragment_consts(p);
