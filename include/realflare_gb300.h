@@ -32,7 +32,7 @@ typedef enum rf_status {
     RF_OK = 0,
     RF_ERR_INVALID_ARG = 1,     /* a size, pointer or setting outside the supported range */
     RF_ERR_OUT_OF_MEMORY = 2,   /* a device allocation requested by the caller failed */
-    RF_ERR_TIMEOUT = 3,         /* a bounded device wait gave up (device error flag set) */
+    /* 3 is not used: no kernel of this library waits on another */
     RF_ERR_CUDA = 4,            /* a CUDA runtime call failed (see rf_last_cuda_error) */
     RF_ERR_WORKSPACE = 5,       /* workspace too small; the required size was written back */
     RF_ERR_NOT_SUPPORTED = 6    /* e.g. a non-power-of-two FFT size */

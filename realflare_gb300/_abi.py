@@ -17,7 +17,6 @@ LIB_PATH = os.path.join(HERE, 'librealflare_gb300.so')
 RF_OK = 0
 RF_ERR_INVALID_ARG = 1
 RF_ERR_OUT_OF_MEMORY = 2
-RF_ERR_TIMEOUT = 3
 RF_ERR_CUDA = 4
 RF_ERR_WORKSPACE = 5
 RF_ERR_NOT_SUPPORTED = 6
