@@ -35,7 +35,7 @@ typedef enum rf_status {
     /* 3 is not used: no kernel of this library waits on another */
     RF_ERR_CUDA = 4,            /* a CUDA runtime call failed (see rf_last_cuda_error) */
     RF_ERR_WORKSPACE = 5,       /* workspace too small; the required size was written back */
-    RF_ERR_NOT_SUPPORTED = 6    /* e.g. a non-power-of-two FFT size */
+    RF_ERR_NOT_SUPPORTED = 6    /* e.g. an FFT side above 4096 */
 } rf_status;
 
 /* One lens element (64 bytes). radius/ior/height/center/coating/coefficients carry the
@@ -231,7 +231,8 @@ int rf_raster_masks(const float* vertexes, const uint64_t* masks, int32_t batch_
 
 /* ---- diffraction ------------------------------------------------------------------ */
 /* In-place 2-D FFT of a batch of complex64 images [batch][height][width] (interleaved
- * re, im), width and height powers of two in [2, 4096]. direction -1 = forward
+ * re, im), width and height any length in [2, 4096] (powers of two by radix-2 passes, other
+ * lengths by Bluestein's chirp-z convolution, as numpy accepts any length). direction -1 = forward
  * (exp(-i...)), +1 = inverse; scale multiplies the result (1/sqrt(wh) = numpy "ortho").
  * Replaces numpy.fft.fft2/fftn/ifftn in realflare/api/tasks/starburst.py:71 and
  * realflare/utils/frft.py:27-60. scratch: device complex64 buffer of the same size. */

@@ -11,7 +11,10 @@
 //  * the ghost texture's fractional Fourier transform (realflare/api/tasks/ghost.py:13-36
 //    and realflare/utils/frft.py:20-62, Ozaktas et al. 1996 chirp convolution), built from
 //    the plain transform and element-wise chirp kernels.
-// Sizes are powers of two from 2 to 4096 per axis.
+// Rows whose length is a power of two run the radix-2 kernel below; any other length from
+// 2 to 4096 runs Bluestein's chirp-z form (Bluestein 1970): with w_m = exp(d pi i m^2 / n),
+// X_k = w_k sum_j (x_j w_j) conj(w_{k-j}), a linear convolution evaluated by radix-2
+// transforms of a power-of-two length M >= 2n - 1, in shared memory, one row per block.
 #include <complex>
 #include <math.h>
 
@@ -100,14 +103,109 @@ __global__ void k_fft_rows(Load load, Store store, int n, int log_n, float dir) 
 }
 
 int log2_exact(int n) {
-    if (n < 2 || n > kMaxN || (n & (n - 1))) return -1;
+    if (n < 2 || n > 2 * kMaxN || (n & (n - 1))) return -1;
     int l = 0;
     while ((1 << l) < n) l++;
     return l;
 }
 
+// lengths the row transforms accept: 2 to 4096, any factorisation
+bool fft_length_ok(int n) { return n >= 2 && n <= kMaxN; }
+
+// exp(d pi i m^2 / n), the phase reduced exactly: m^2 mod 2n
+__device__ __forceinline__ float2 bluestein_chirp(int m, int n, float d) {
+    const long long r = ((long long)m * m) % (2LL * n);
+    float sn, cs;
+    sincospif(d * (float)r / (float)n, &sn, &cs);
+    return make_float2(cs, sn);
+}
+
+// the radix-2 butterflies of k_fft_rows over two arrays at once (input in bit-reversed order,
+// output in natural order), twiddles tw[k] = exp(-2 pi i k / M)
+__device__ __forceinline__ void butterflies2(float2* x, float2* y, const float2* tw, int M, int logM) {
+    for (int s = 1; s <= logM; s++) {
+        const int half = 1 << (s - 1);
+        const int stride = M >> s;
+        for (int k = threadIdx.x; k < M / 2; k += blockDim.x) {
+            const int j = k & (half - 1);
+            const int base = (k >> (s - 1)) << s;
+            const float2 w = tw[j * stride];
+            float2 u = x[base + j], v = cmul(x[base + j + half], w);
+            x[base + j] = make_float2(u.x + v.x, u.y + v.y);
+            x[base + j + half] = make_float2(u.x - v.x, u.y - v.y);
+            if (y) {
+                u = y[base + j];
+                v = cmul(y[base + j + half], w);
+                y[base + j] = make_float2(u.x + v.x, u.y + v.y);
+                y[base + j + half] = make_float2(u.x - v.x, u.y - v.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// One row of any length n (Bluestein): a_j = x_j w_j and b_m = conj(w_m) for |m| < n
+// (wrapped to M - m), A = FFT(a), B = FFT(b), conv = IFFT(A B) (as conj(FFT(conj(A B))) / M),
+// X_k = w_k conv_k. Shared memory: a, b (M each) and the twiddles (M / 2).
+template <class Load, class Store>
+__global__ void k_fft_rows_bluestein(Load load, Store store, int n, int M, int logM, float dir) {
+    extern __shared__ float2 sm[];
+    float2* a = sm;
+    float2* b = a + M;
+    float2* tw = b + M;
+    const long long row = blockIdx.x;
+    for (int k = threadIdx.x; k < M / 2; k += blockDim.x) {
+        float sn, cs;
+        sincospif(-2.0f * (float)k / (float)M, &sn, &cs);
+        tw[k] = make_float2(cs, sn);
+    }
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+        float2 av = make_float2(0.0f, 0.0f), bv = make_float2(0.0f, 0.0f);
+        if (i < n) {
+            const float2 w = bluestein_chirp(i, n, dir);
+            av = cmul(load(row, i), w);
+            bv = make_float2(w.x, -w.y);
+        } else if (i > M - n) {
+            const float2 w = bluestein_chirp(M - i, n, dir);
+            bv = make_float2(w.x, -w.y);
+        }
+        const int rev = (int)(__brev((unsigned)i) >> (32 - logM));
+        a[rev] = av;
+        b[rev] = bv;
+    }
+    __syncthreads();
+    butterflies2(a, b, tw, M, logM);
+    for (int i = threadIdx.x; i < M; i += blockDim.x) a[i] = cmul(a[i], b[i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+        const float2 v = a[i];
+        b[(int)(__brev((unsigned)i) >> (32 - logM))] = make_float2(v.x, -v.y);
+    }
+    __syncthreads();
+    butterflies2(b, nullptr, tw, M, logM);
+    const float inv = 1.0f / (float)M;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 c = make_float2(b[k].x * inv, -b[k].y * inv);
+        store(row, k, cmul(bluestein_chirp(k, n, dir), c));
+    }
+}
+
 template <class Load, class Store>
 int launch_rows(Load load, Store store, long long rows, int n, float dir, cudaStream_t s) {
+    if (!fft_length_ok(n)) return RF_ERR_NOT_SUPPORTED;
+    if (n & (n - 1)) {
+        int M = 1;
+        while (M < 2 * n - 1) M <<= 1;
+        const int logM = log2_exact(M);
+        const size_t smem = sizeof(float2) * (2 * M + M / 2);
+        auto kernel = k_fft_rows_bluestein<Load, Store>;
+        if (smem > 48 * 1024)
+            RF_TRY(cuda_status(
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
+        kernel<<<(unsigned)rows, M / 2 < 256 ? (M / 2 < 32 ? 32 : M / 2) : 256, smem, s>>>(load, store, n, M, logM,
+                                                                                            dir);
+        return launch_status();
+    }
     const int log_n = log2_exact(n);
     const int threads = n / 2 < 256 ? (n / 2 < 32 ? 32 : n / 2) : 256;
     const size_t smem = sizeof(float2) * (n + n / 2);
@@ -126,11 +224,12 @@ int fft2(float2* data, float2* scratch, int batch, int w, int h, int direction, 
 }
 
 // ---------------------------------------------------------------- FRFT helpers
+// numpy's fftshift moves element i to (i + n / 2) mod n: output i reads (i + n - n / 2) mod n
 __global__ void k_fftshift_real(const float* __restrict__ in, float2* __restrict__ out, int w, int h) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)w * h) return;
     const int y = (int)(i / w), x = (int)(i % w);
-    out[i] = make_float2(in[(size_t)((y + h / 2) % h) * w + (x + w / 2) % w], 0.0f);
+    out[i] = make_float2(in[(size_t)((y + h - h / 2) % h) * w + (x + w - w / 2) % w], 0.0f);
 }
 
 __global__ void k_flip(const float2* __restrict__ in, float2* __restrict__ out, int w, int h) {
@@ -169,7 +268,7 @@ __global__ void k_frft_finish(const float2* __restrict__ data, float* __restrict
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)w * h) return;
     const int y = (int)(i / w), x = (int)(i % w);
-    const int ys = (y + h / 2) % h, xs = (x + w / 2) % w;  // fftshift source
+    const int ys = (y + h - h / 2) % h, xs = (x + w - w / 2) % w;  // fftshift source
     float s, co;
     sincospif(chirp_r(ys, xs, w, h) * c1, &s, &co);
     float2 v = cmul(cmul(scale, make_float2(co, s)), data[(size_t)ys * w + xs]);
@@ -183,7 +282,7 @@ extern "C" int rf_fft2(float* data, float* scratch, int32_t batch, int32_t width
                        float scale, void* stream) {
     using namespace rf;
     if (!data || !scratch || batch < 1) return RF_ERR_INVALID_ARG;
-    if (log2_exact(width) < 0 || log2_exact(height) < 0) return RF_ERR_NOT_SUPPORTED;
+    if (!fft_length_ok(width) || !fft_length_ok(height)) return RF_ERR_NOT_SUPPORTED;
     return fft2((float2*)data, (float2*)scratch, batch, width, height, direction, scale, (cudaStream_t)stream);
 }
 
@@ -192,7 +291,7 @@ extern "C" int rf_starburst_spectrum(const float* aperture, int32_t width, int32
                                      void* stream) {
     using namespace rf;
     if (!aperture || !lambdas_mm || !scratch || !spectrum || count < 1 || count > 256) return RF_ERR_INVALID_ARG;
-    if (log2_exact(width) < 0 || log2_exact(height) < 0) return RF_ERR_NOT_SUPPORTED;
+    if (!fft_length_ok(width) || !fft_length_ok(height)) return RF_ERR_NOT_SUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     // phase = pi * (x^2 + y^2) / (lambda d): one factor per wavelength, passed by value
     LoadStarburst load;
@@ -211,7 +310,7 @@ extern "C" int rf_ghost_frft(const float* aperture, int32_t width, int32_t heigh
                              float* texture, void* stream) {
     using namespace rf;
     if (!aperture || !scratch || !texture) return RF_ERR_INVALID_ARG;
-    if (log2_exact(width) < 0 || log2_exact(height) < 0) return RF_ERR_NOT_SUPPORTED;
+    if (!fft_length_ok(width) || !fft_length_ok(height)) return RF_ERR_NOT_SUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     const long long n = (long long)width * height;
     float2* A = (float2*)scratch;

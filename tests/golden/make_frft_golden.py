@@ -36,6 +36,8 @@ CASES = [
     ('s64', 64, 64, 6, 0.05, (0.0, 8.0, 32.0, 64.0, 100.0, 150.0, 275.0, 330.0)),
     ('s256', 256, 256, 8, 0.0, (0.0, 64.0, 275.0)),
     ('r64x128', 64, 128, 5, 0.02, (8.0, 150.0)),
+    # lengths that are not powers of two, one odd (numpy's fftshift moves by n // 2)
+    ('r75x120', 75, 120, 7, 0.03, (8.0, 150.0, 275.0)),
 ]
 
 

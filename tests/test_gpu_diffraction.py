@@ -31,7 +31,10 @@ def oracle():
     return Oracle('f32')
 
 
-@pytest.mark.parametrize('shape', [(8, 16), (64, 64), (256, 128), (512, 512)])
+# powers of two (radix-2 passes) and other lengths (Bluestein's chirp-z form): odd, even,
+# mixed with a power of two, and the longest row (4095: an 8192-point convolution)
+@pytest.mark.parametrize('shape', [(8, 16), (64, 64), (256, 128), (512, 512), (5, 7), (300, 300), (75, 128),
+                                   (3, 4095)])
 @pytest.mark.parametrize('direction', [-1, 1])
 def test_fft2_matches_numpy(shape, direction):
     h, w = shape
@@ -44,7 +47,9 @@ def test_fft2_matches_numpy(shape, direction):
     torch.cuda.synchronize()
     got = data.cpu().numpy().view(np.complex64)
     ref = (np.fft.fftn if direction < 0 else np.fft.ifftn)(x.astype(np.complex128), axes=(1, 2), norm='ortho')
-    assert rel_l2(got.view(np.float32), ref.astype(np.complex64).view(np.float32)) < 2e-6
+    pow2 = all(n & (n - 1) == 0 for n in shape)
+    # the chirp-z form rounds through three transforms of twice the length
+    assert rel_l2(got.view(np.float32), ref.astype(np.complex64).view(np.float32)) < (2e-6 if pow2 else 1e-5)
 
 
 def aperture_image(oracle, n=128, blades=8):
@@ -87,7 +92,7 @@ def test_aperture_dust_and_noise_dust_match_oracle(oracle):
     assert rel_l2(img2.cpu().numpy(), ref2) < 1e-5
 
 
-@pytest.mark.parametrize('n', [64, 256])
+@pytest.mark.parametrize('n', [64, 256, 300])
 def test_starburst_spectrum_matches_numpy(oracle, n):
     from oracle.oracle import fft_power_spectrum
 
