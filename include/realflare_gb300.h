@@ -329,6 +329,7 @@ typedef struct rf_frame {
     int32_t tile_offset, tile_count;  /* the frame's raster tiles in the batch's tile numbering */
     float direction_n[3];     /* normalize(-direction.xyz) in FP32, as rf_trace computes it */
     int32_t pad1;
+    uint64_t ghost_texture;   /* rf_ghost_texture_object of the frame's ghost texture, or 0 */
 } rf_frame;
 
 typedef struct rf_batch_sizes {
@@ -338,7 +339,7 @@ typedef struct rf_batch_sizes {
     int64_t image_pixels, ghost_floats;
     int32_t max_colors, max_sub;  /* largest max(W-1,1) * WS and WS over the frames */
     int32_t max_sub_steps;        /* largest anti-aliasing sample count over the frames */
-    int32_t pad;
+    int32_t ghost_textures;       /* 1 when every frame has a ghost texture object */
 } rf_batch_sizes;
 
 /* Checks every frame and fills the derived fields of frames (host memory) and sizes.
@@ -377,6 +378,15 @@ int rf_bin_tiles_batch(const rf_frame* frames, const rf_batch_sizes* sizes, cons
 /* rf_raster of every frame in one persistent launch: CTAs take tiles from a device-side
  * queue (heaviest first) until it is empty. ghosts: the concatenated ghost textures;
  * images: float[4 * image_pixels]; workspace: the one given to rf_bin_tiles_batch. */
+/* A texture object over a ghost texture (device float[height][width]) for the raster's ghost
+ * lookups (no counterpart in the reference: its rasteriser reads an OpenCL image,
+ * rasterizing.cl:483-485): created once per device, address and size and kept by the library.
+ * *texture = 0 when the address or the row pitch (width * 4 bytes) is not aligned as the
+ * device's textures require; the raster then loads the texels. rf_raster and
+ * rf_raster_ordered use it by themselves; a batch passes it per frame in
+ * rf_frame.ghost_texture. */
+int rf_ghost_texture_object(const float* ghost, int32_t width, int32_t height, uint64_t* texture);
+
 int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* vertexes,
                     const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
                     const float* spectrum, void* workspace, size_t workspace_bytes,

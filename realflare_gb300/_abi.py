@@ -108,6 +108,7 @@ class Frame(ctypes.Structure):
         ('tile_count', ctypes.c_int32),
         ('direction_n', ctypes.c_float * 3),
         ('pad1', ctypes.c_int32),
+        ('ghost_texture', ctypes.c_uint64),
     ]
 
 
@@ -132,7 +133,7 @@ class BatchSizes(ctypes.Structure):
         ('max_colors', ctypes.c_int32),
         ('max_sub', ctypes.c_int32),
         ('max_sub_steps', ctypes.c_int32),
-        ('pad', ctypes.c_int32),
+        ('ghost_textures', ctypes.c_int32),
     ]
 
 
@@ -179,6 +180,7 @@ SIGNATURES = {
     'rf_vertex_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P],
     'rf_batch_workspace_size': [ctypes.POINTER(BatchSizes), I64, ctypes.POINTER(ctypes.c_size_t)],
     'rf_bin_tiles_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, ctypes.c_size_t, P, P, I64, P, P],
+    'rf_ghost_texture_object': [P, I32, I32, ctypes.POINTER(ctypes.c_uint64)],
     'rf_raster_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P, P, P, ctypes.c_size_t, I64, P, P, P],
 }
 

@@ -66,7 +66,10 @@ class _Inputs:
     wavelengths: np.ndarray
 
 
-def _frame_inputs(projects: list, ghost_offsets: list, ghost_shapes: list) -> _Inputs:
+def _frame_inputs(projects: list, ghost_offsets: list, ghost_shapes: list,
+                  ghosts: torch.Tensor | None = None) -> _Inputs:
+    """The frames' rf_frame records; with ``ghosts`` (the device buffer of the ghost textures)
+    each frame also gets the texture object of its ghost texture."""
     frames = (Frame * len(projects))()
     elements, paths, wavelengths = [], [], []
     n_el = n_pa = n_wl = 0
@@ -81,6 +84,12 @@ def _frame_inputs(projects: list, ghost_offsets: list, ghost_shapes: list) -> _I
         f.area_orig, f.min_area = prepare.quad_constants(p)
         f.element_offset, f.path_offset, f.wavelength_offset = n_el, n_pa, n_wl
         f.ghost_offset = ghost_offsets[i]
+        if ghosts is not None:
+            tex = ctypes.c_uint64()
+            h, w = ghost_shapes[i]
+            check(lib().rf_ghost_texture_object(ptr(ghosts) + 4 * int(ghost_offsets[i]), w, h, ctypes.byref(tex)),
+                  'rf_ghost_texture_object')
+            f.ghost_texture = tex.value
         elements.append(ti.elements)
         paths.append(ti.paths)
         wavelengths.append(ti.wavelengths)
@@ -120,7 +129,7 @@ class BatchRenderer:
         with torch.cuda.stream(self.stream):
             self.ghosts, ghost_offsets, ghost_shapes = ghosts if ghosts is not None else ghost_textures(
                 self.projects, self.stream)
-            inputs = _frame_inputs(self.projects, ghost_offsets, ghost_shapes)
+            inputs = _frame_inputs(self.projects, ghost_offsets, ghost_shapes, self.ghosts)
             self.sizes = BatchSizes()
             check(self.lib.rf_batch_plan(inputs.frames, len(self.projects), tile_size, rays_per_thread,
                                          ctypes.byref(self.sizes)), 'rf_batch_plan')

@@ -100,6 +100,8 @@ extern "C" int rf_batch_plan(rf_frame* frames, int32_t frame_count, int32_t tile
         f.direction_n[2] = vz * inv;
         f.pad1 = 0;
     }
+    z.ghost_textures = 1;
+    for (int i = 0; i < frame_count; i++) z.ghost_textures = z.ghost_textures && frames[i].ghost_texture != 0;
     if (tiles > (1LL << 30) || z.trace_blocks > 0x7fffffffLL || z.vertex_blocks > 0x7fffffffLL ||
         z.pair_blocks > 0x7fffffffLL || z.quad_blocks > 0x7fffffffLL) {
         set_error_text("rf_batch_plan: the batch exceeds 2^31 blocks or 2^30 tiles in one stage");

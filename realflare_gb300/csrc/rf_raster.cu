@@ -25,6 +25,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
+#include <vector>
 
 #include "rf_common.cuh"
 
@@ -97,6 +99,7 @@ struct RasterParams {
     float intensity, ghost_scale;
     int ghost_w, ghost_h;
     bool safe_screen;
+    unsigned long long ghost_tex;  // texture object over the ghost texture (the kTex kernels)
 };
 
 __device__ __forceinline__ bool top_left(int ax, int ay, int bx, int by) {
@@ -266,17 +269,33 @@ __device__ __forceinline__ float ghost_sample(const float* __restrict__ tex, int
     return fmaf(b, bottom - top, top);
 }
 
+// ghost_sample through a texture object over the same texels (float, pitch-linear, border
+// address mode): tex2Dgather at the centre of the 2 x 2 footprint, (i0 + 1, j0 + 1), exactly
+// half a texel from every footprint boundary, returns texels (i0, j0 + 1), (i0 + 1, j0 + 1),
+// (i0 + 1, j0), (i0, j0) in x, y, z, w, and 0 for texels outside the image; one texture
+// instruction instead of the bounds test, the address arithmetic and four loads. The values,
+// and so the interpolation, are ghost_sample's.
+__device__ __forceinline__ float ghost_sample_tex(unsigned long long tex, float u, float v) {
+    if (!(fabsf(u) + fabsf(v) < 2e9f)) return 0.0f;  // non-finite or far outside
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const float4 g = tex2Dgather<float4>((cudaTextureObject_t)tex, fu + 1.0f, fv + 1.0f, 0);
+    const float top = fmaf(a, g.z - g.w, g.w), bottom = fmaf(a, g.y - g.x, g.x);
+    return fmaf(b, bottom - top, top);
+}
+
 // fragment_shader (rasterizing.cl:471-506) times the hit count. The texture coordinate
 // ((uv / scale + 1) / 2) * size - 0.5 is evaluated as uv * tex_scale + tex_offset.
 struct FragmentConsts {
     float tsx, tox, tsy, toy;  // texel coordinate scale and offset per axis
 };
+template <bool kTex = false>
 __device__ __forceinline__ float fragment_fast(const Rec& r, const float w[4], const float* __restrict__ ghost,
                                                const RasterParams& p, const FragmentConsts& fc, int hits) {
     const float4 uv01 = ld4(r.uv), uv23 = ld4(r.uv + 4);
     const float u = w[0] * uv01.x + w[1] * uv01.z + w[2] * uv23.x + w[3] * uv23.z;
     const float v = w[0] * uv01.y + w[1] * uv01.w + w[2] * uv23.y + w[3] * uv23.w;
-    const float gi = ghost_sample(ghost, p.ghost_w, p.ghost_h, u, v);
+    const float gi = kTex ? ghost_sample_tex(p.ghost_tex, u, v) : ghost_sample(ghost, p.ghost_w, p.ghost_h, u, v);
     // smoothstep(1, 0.95, rrel): the ramp (rrel - 1) / (0.95 - 1) is linear in rrel, so the
     // corners' ramps interpolate to the fragment's (the weights sum to one)
     const float4 rl = ld4(r.rs);
@@ -418,8 +437,9 @@ constexpr size_t raster_smem_bytes(int maxW, int WS) {
 
 // Tile (tx, ty), whose entries are tile_entries[begin, end). smem4 holds the dynamic shared
 // memory (raster_smem_bytes), next_block two shared counters. kS: the anti-aliasing sample
-// count when known at compile time (1), else 0 (p.S).
-template <int T, int kS>
+// count when known at compile time (1), else 0 (p.S). kTex: sample the ghost texture through
+// p.ghost_tex.
+template <int T, int kS, bool kTex = false>
 __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint32_t begin, uint32_t end,
                                             const uint32_t* __restrict__ tile_entries,
                                             const float* __restrict__ ghost, const float* __restrict__ spectrum,
@@ -589,7 +609,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                             if (lane == __ffs(__activemask()) - 1) st_steps++;)
                     float wt[4];
                     barycentric_fast(r, fx, fy, wt);
-                    const float f = fragment_fast(r, wt, ghost, p, fc, 1);
+                    const float f = fragment_fast<kTex>(r, wt, ghost, p, fc, 1);
                     const float4 col = *reinterpret_cast<const float4*>(r.col);
                     r0 += col.x * f;
                     r1 += col.y * f;
@@ -624,7 +644,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
                         const unsigned am = __activemask();
                         if (__all_sync(am, z) && lane == __ffs(am) - 1) st_zero_iter++;
                     })
-                    const float f = fragment_fast(r, wt, ghost, p, fc, kS == 1 ? 1 : hits);
+                    const float f = fragment_fast<kTex>(r, wt, ghost, p, fc, kS == 1 ? 1 : hits);
                     const float4 col = *reinterpret_cast<const float4*>(r.col);
                     r0 += col.x * f;
                     r1 += col.y * f;
@@ -663,7 +683,7 @@ __device__ __forceinline__ void raster_tile(const float4* __restrict__ vtx, uint
 // One CTA per tile of a frame: CTA k shades tile order[k], or tile k without an order.
 // CTAs start in index order as slots free up, so an order by decreasing work starts the
 // heaviest tiles first and ends the launch with light ones.
-template <int T, int kS>
+template <int T, int kS, bool kTex>
 __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : RF_RASTER_MIN_BLOCKS)
     k_raster(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
              const uint32_t* __restrict__ tile_entries, const uint32_t* __restrict__ order,
@@ -672,16 +692,17 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : 
     extern __shared__ float4 smem4[];
     __shared__ int next_block[2];  // blocks of each buffer's batch handed out so far
     const int tile = order ? (int)order[blockIdx.x] : (int)blockIdx.x;
-    raster_tile<T, kS>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs, image,
-                   tile % p.ntx, tile / p.ntx, smem4, next_block);
+    raster_tile<T, kS, kTex>(vtx, tile_offsets[tile], tile_offsets[tile + 1], tile_entries, ghost, spectrum, p, fcs,
+                             image, tile % p.ntx, tile / p.ntx, smem4, next_block);
 }
 
 __host__ __device__ inline bool make_params(const rf_raster_args& a, RasterParams& p);
 __host__ __device__ inline FragmentConsts fragment_consts(const RasterParams& p);
 
 // Every frame of a batch in one persistent launch: each CTA takes the next tile from the
-// queue (tiles ordered by decreasing entry count) until none are left.
-template <int T, int kS>
+// queue (tiles ordered by decreasing entry count) until none are left. kTex: every frame's
+// ghost lookups go through its rf_frame.ghost_texture.
+template <int T, int kS, bool kTex>
 __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : RF_RASTER_MIN_BLOCKS)
     k_raster_batch(const rf_frame* __restrict__ frames, int F, int tiles, const uint32_t* __restrict__ order,
                    unsigned* __restrict__ queue, const unsigned long long* __restrict__ entry_total,
@@ -705,6 +726,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : 
                 const rf_frame& fr = frames[f];
                 RasterParams q;
                 make_params(fr.raster, q);
+                if (kTex) q.ghost_tex = fr.ghost_texture;
                 q.T = T;
                 q.ntx = (q.width + T - 1) / T;
                 sp = q;
@@ -719,7 +741,7 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? RF_RASTER_MIN_BLOCKS_S1 : 
         __syncthreads();
         if (item >= tiles) break;
         const int gt = s_gt, tile = s_tile;
-        raster_tile<T, kS>(vtx_all + 2 * s_vtx, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
+        raster_tile<T, kS, kTex>(vtx_all + 2 * s_vtx, tile_offsets[gt], tile_offsets[gt + 1], tile_entries,
                            ghosts + s_ghost, spectrum, sp, sfc, images + s_image, tile % sp.ntx, tile / sp.ntx, smem4,
                            next_block);
         __syncthreads();  // the tile's accumulators and `item` are free again
@@ -749,6 +771,21 @@ __device__ __forceinline__ float ghost_sample_grad(const float* __restrict__ tex
     return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
 }
 
+// ghost_sample_grad with the four texels from one gather of the ghost texture's texture object
+// (border mode: texels outside the texture read 0, as the loads' bounds checks give).
+__device__ __forceinline__ float ghost_sample_grad_tex(unsigned long long tex, float u, float v, float& du,
+                                                       float& dv) {
+    du = dv = 0.0f;
+    if (!(fabsf(u) < 1e9f) || !(fabsf(v) < 1e9f)) return 0.0f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const float4 g = tex2Dgather<float4>((cudaTextureObject_t)tex, fu + 1.0f, fv + 1.0f, 0);
+    const float t00 = g.w, t10 = g.z, t01 = g.x, t11 = g.y;
+    du = (1.0f - b) * (t10 - t00) + b * (t11 - t01);
+    dv = (1.0f - a) * (t01 - t00) + a * (t11 - t10);
+    return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
+}
+
 constexpr int kGradAttrs = 5;  // per corner: u, v, rrel, reflectance, intensity
 // row stride of the backward's per-warp transpose buffers (floats)
 constexpr int kRedStride = 36;
@@ -762,8 +799,9 @@ __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6}
 // vertex positions), differentiating each fragment with respect to the attributes its
 // corners interpolate. Per record the warp sums its pixels' contributions with shuffles;
 // the CTA sums warps in shared memory and adds each record's totals to the two vertices
-// (wavelength pair endpoints) of each corner once per tile.
-template <int T, int kS>
+// (wavelength pair endpoints) of each corner once per tile. kTex: the ghost lookups gather
+// from the texture object p.ghost_tex.
+template <int T, int kS, bool kTex>
 __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
     k_raster_backward(const float4* __restrict__ vtx, const uint32_t* __restrict__ tile_offsets,
                       const uint32_t* __restrict__ tile_entries, const float* __restrict__ ghost,
@@ -954,7 +992,8 @@ __global__ void __launch_bounds__(kThreads, kS == 1 ? 3 : 2)
                         const float u = wt[0] * uv01.x + wt[1] * uv01.z + wt[2] * uv23.x + wt[3] * uv23.z;
                         const float v = wt[0] * uv01.y + wt[1] * uv01.w + wt[2] * uv23.y + wt[3] * uv23.w;
                         float dgu, dgv;
-                        const float gi = ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u, v, dgu, dgv);
+                        const float gi = kTex ? ghost_sample_grad_tex(p.ghost_tex, u, v, dgu, dgv)
+                                              : ghost_sample_grad(ghost, p.ghost_w, p.ghost_h, u, v, dgu, dgv);
                         const float4 rl = ld4(r.rs);
                         const float st = __saturatef(wt[0] * rl.x + wt[1] * rl.y + wt[2] * rl.z + wt[3] * rl.w);
                         const float ri = st * st * (3.0f - 2.0f * st);
@@ -1127,6 +1166,7 @@ __host__ __device__ inline bool make_params(const rf_raster_args& a, RasterParam
     p.ghost_w = a.ghost_width;
     p.ghost_h = a.ghost_height;
     p.safe_screen = (float)a.width * a.sub_steps <= 16384.0f && (float)a.height * a.sub_steps <= 16384.0f;
+    p.ghost_tex = 0;  // the texels are loaded unless a launcher sets a texture object
     return true;
 }
 
@@ -1145,17 +1185,87 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
     return RF_OK;
 }
 
+// A texture object over a caller's ghost texture (float texels, pitch w * 4 bytes, border
+// address mode, point filtering, unnormalised coordinates) for ghost_sample_tex, created once
+// per device, address and size and kept (a handful of descriptors; past 256 the device is
+// synchronised and the cache cleared, so no kernel can still be using one). 0 when the
+// address or the row pitch is not aligned as textures require; the raster then loads texels.
+unsigned long long ghost_texture_object(const float* ghost, int w, int h) {
+    struct Entry {
+        int dev;
+        const float* ptr;
+        int w, h;
+        cudaTextureObject_t obj;
+    };
+    static std::mutex mutex;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lock(mutex);
+    for (const Entry& e : cache)
+        if (e.dev == dev && e.ptr == ghost && e.w == w && e.h == h) return e.obj;
+    // the row pitch must be a multiple of the texture pitch alignment, the base address a
+    // multiple of the texture alignment
+    int pitch_align = 0, base_align = 0;
+    if (cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&base_align, cudaDevAttrTextureAlignment, dev) != cudaSuccess || pitch_align <= 0 ||
+        base_align <= 0)
+        return 0;
+    if (((size_t)w * sizeof(float)) % (size_t)pitch_align != 0 || (uintptr_t)ghost % (uintptr_t)base_align != 0)
+        return 0;
+    if (cache.size() >= 256) {
+        if (cudaDeviceSynchronize() != cudaSuccess) return 0;
+        for (const Entry& e : cache) {
+            int cur = 0;
+            cudaGetDevice(&cur);
+            cudaSetDevice(e.dev);
+            cudaDestroyTextureObject(e.obj);
+            cudaSetDevice(cur);
+        }
+        cache.clear();
+    }
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypePitch2D;
+    rd.res.pitch2D.devPtr = const_cast<float*>(ghost);
+    rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
+    rd.res.pitch2D.width = (size_t)w;
+    rd.res.pitch2D.height = (size_t)h;
+    rd.res.pitch2D.pitchInBytes = (size_t)w * sizeof(float);
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t obj = 0;
+    if (cudaCreateTextureObject(&obj, &rd, &td, nullptr) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    cache.push_back({dev, ghost, w, h, obj});
+    return obj;
+}
+
 template <int T, int kS>
 int launch_raster_s(const float* vertexes, const uint32_t* offsets, const uint32_t* entries, const uint32_t* order,
                     const float* ghost, const float* spectrum, RasterParams p, float* image, cudaStream_t s) {
     static std::atomic<size_t> allowed[kMaxDevices];
+    static std::atomic<size_t> allowed_tex[kMaxDevices];
     p.T = T;
     p.ntx = (p.width + T - 1) / T;
     const int nty = (p.height + T - 1) / T;
     const size_t smem = raster_smem_bytes<T>(p.maxW, p.WS);
-    RF_TRY(allow_smem(k_raster<T, kS>, smem, allowed));
-    k_raster<T, kS><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, order, ghost,
-                                                       spectrum, p, fragment_consts(p), (float4*)image);
+    p.ghost_tex = ghost_texture_object(ghost, p.ghost_w, p.ghost_h);
+    if (p.ghost_tex) {
+        RF_TRY(allow_smem(k_raster<T, kS, true>, smem, allowed_tex));
+        k_raster<T, kS, true><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, order,
+                                                                 ghost, spectrum, p, fragment_consts(p),
+                                                                 (float4*)image);
+    } else {
+        RF_TRY(allow_smem(k_raster<T, kS, false>, smem, allowed));
+        k_raster<T, kS, false><<<p.ntx * nty, kThreads, smem, s>>>((const float4*)vertexes, offsets, entries, order,
+                                                                  ghost, spectrum, p, fragment_consts(p),
+                                                                  (float4*)image);
+    }
     return launch_status();
 }
 
@@ -1166,7 +1276,7 @@ int launch_raster(const float* vertexes, const uint32_t* offsets, const uint32_t
     return launch_raster_s<T, 0>(vertexes, offsets, entries, order, ghost, spectrum, p, image, s);
 }
 
-template <int T, int kS>
+template <int T, int kS, bool kTex>
 int launch_raster_batch(const rf_frame* frames, const rf_batch_sizes& z, const float* vertexes,
                         const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
                         const float* spectrum, const BatchWorkspace& w, long long capacity,
@@ -1176,20 +1286,20 @@ int launch_raster_batch(const rf_frame* frames, const rf_batch_sizes& z, const f
     // the largest frame layout: 3 * max(W-1,1) * WS colours, WS blend weights (rounded to 4)
     const size_t smem = sizeof(Rec) * 2 * kBatchRecords + sizeof(float) * (3 * z.max_colors + ((z.max_sub + 3) & ~3)) +
                         sizeof(float) * 96 * (T * T / 32);
-    RF_TRY(allow_smem(k_raster_batch<T, kS>, smem, allowed));
+    RF_TRY(allow_smem(k_raster_batch<T, kS, kTex>, smem, allowed));
     int dev = 0, sms = 0;
     RF_TRY(cuda_status(cudaGetDevice(&dev)));
     RF_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)));
     int per_sm = ctas_per_sm[dev].load();
     if (per_sm == 0) {
         RF_TRY(cuda_status(
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_batch<T, kS>, kThreads, smem)));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_batch<T, kS, kTex>, kThreads, smem)));
         per_sm = per_sm > 0 ? per_sm : 1;
         ctas_per_sm[dev].store(per_sm);
     }
     const long long ctas = std::min<long long>((long long)sms * per_sm, z.tiles);
     RF_TRY(cuda_status(cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), s)));
-    k_raster_batch<T, kS><<<(unsigned)ctas, kThreads, smem, s>>>(
+    k_raster_batch<T, kS, kTex><<<(unsigned)ctas, kThreads, smem, s>>>(
         frames, z.frame_count, z.tiles, batch_tile_order(w, z), w.queue, (const unsigned long long*)entry_total,
         capacity, (const float4*)vertexes, tile_offsets, tile_entries, ghosts, spectrum, (float4*)images);
     return launch_status();
@@ -1214,20 +1324,28 @@ extern "C" int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* siz
     if (w.bytes > workspace_bytes) return RF_ERR_INVALID_ARG;
     const bool one = z.max_sub_steps <= 1;  // every frame takes one sample per pixel
     cudaStream_t s = (cudaStream_t)stream;
+#define RF_BATCH_LAUNCH(T, S, X)                                                                              \
+    launch_raster_batch<T, S, X>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum, w, entry_capacity, \
+                                 entry_total, images, s)
+    const bool tex = z.ghost_textures != 0;
     switch (z.tile_size) {
         case 32:
-            return one ? launch_raster_batch<32, 1>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
-                                                    w, entry_capacity, entry_total, images, s)
-                       : launch_raster_batch<32, 0>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
-                                                    w, entry_capacity, entry_total, images, s);
+            return one ? (tex ? RF_BATCH_LAUNCH(32, 1, true) : RF_BATCH_LAUNCH(32, 1, false))
+                       : (tex ? RF_BATCH_LAUNCH(32, 0, true) : RF_BATCH_LAUNCH(32, 0, false));
         case 16:
-            return one ? launch_raster_batch<16, 1>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
-                                                    w, entry_capacity, entry_total, images, s)
-                       : launch_raster_batch<16, 0>(frames, z, vertexes, tile_offsets, tile_entries, ghosts, spectrum,
-                                                    w, entry_capacity, entry_total, images, s);
+            return one ? (tex ? RF_BATCH_LAUNCH(16, 1, true) : RF_BATCH_LAUNCH(16, 1, false))
+                       : (tex ? RF_BATCH_LAUNCH(16, 0, true) : RF_BATCH_LAUNCH(16, 0, false));
+#undef RF_BATCH_LAUNCH
         default:
             return RF_ERR_NOT_SUPPORTED;
     }
+}
+
+extern "C" int rf_ghost_texture_object(const float* ghost, int32_t width, int32_t height, uint64_t* texture) {
+    using namespace rf;
+    if (!ghost || !texture || width < 1 || height < 1) return RF_ERR_INVALID_ARG;
+    *texture = ghost_texture_object(ghost, width, height);
+    return RF_OK;
 }
 
 namespace {
@@ -1306,27 +1424,26 @@ extern "C" int rf_raster_backward(const float* vertexes, const uint32_t* tile_of
     const FragmentConsts fc = fragment_consts(p);
     const float4 *im = (const float4*)image, *gim = (const float4*)grad_image;
     const unsigned grid = (unsigned)(p.ntx * nty);
+    p.ghost_tex = ghost_texture_object(ghost, p.ghost_w, p.ghost_h);
+#define RF_BACKWARD_LAUNCH(TT, SS, X)                                                                         \
+    do {                                                                                                      \
+        static std::atomic<size_t> allowed[kMaxDevices];                                                      \
+        RF_TRY(allow_smem(k_raster_backward<TT, SS, X>, smem, allowed));                                      \
+        k_raster_backward<TT, SS, X><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets,       \
+                                                                  tile_entries, ghost, spectrum, p, fc, im, gim, \
+                                                                  grad_vertexes);                             \
+    } while (0)
+    const bool tex = p.ghost_tex != 0;
     if (T == 32 && p.S == 1) {
-        static std::atomic<size_t> allowed[kMaxDevices];
-        RF_TRY(allow_smem(k_raster_backward<32, 1>, smem, allowed));
-        k_raster_backward<32, 1><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+        if (tex) RF_BACKWARD_LAUNCH(32, 1, true); else RF_BACKWARD_LAUNCH(32, 1, false);
     } else if (T == 32) {
-        static std::atomic<size_t> allowed[kMaxDevices];
-        RF_TRY(allow_smem(k_raster_backward<32, 0>, smem, allowed));
-        k_raster_backward<32, 0><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+        if (tex) RF_BACKWARD_LAUNCH(32, 0, true); else RF_BACKWARD_LAUNCH(32, 0, false);
     } else if (p.S == 1) {
-        static std::atomic<size_t> allowed[kMaxDevices];
-        RF_TRY(allow_smem(k_raster_backward<16, 1>, smem, allowed));
-        k_raster_backward<16, 1><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+        if (tex) RF_BACKWARD_LAUNCH(16, 1, true); else RF_BACKWARD_LAUNCH(16, 1, false);
     } else {
-        static std::atomic<size_t> allowed[kMaxDevices];
-        RF_TRY(allow_smem(k_raster_backward<16, 0>, smem, allowed));
-        k_raster_backward<16, 0><<<grid, kThreads, smem, s>>>((const float4*)vertexes, tile_offsets, tile_entries,
-                                                              ghost, spectrum, p, fc, im, gim, grad_vertexes);
+        if (tex) RF_BACKWARD_LAUNCH(16, 0, true); else RF_BACKWARD_LAUNCH(16, 0, false);
     }
+#undef RF_BACKWARD_LAUNCH
     return launch_status();
 }
 

@@ -69,6 +69,15 @@ def test_plan_lays_frames_out_back_to_back(L, projects, tile, rpt):
     assert (z.trace_blocks, z.quad_blocks, z.vertex_blocks, z.pair_blocks, z.tiles) == (tb, qb, vb, pb, tiles)
     assert z.image_pixels == pix and z.frame_count == len(projects)
     assert z.max_sub == 1 and z.max_colors == max(max(f.trace.wavelength_count - 1, 1) for f in inp.frames)
+    # texture lookups only when every frame has a ghost texture object
+    assert z.ghost_textures == 0
+    for k, f in enumerate(inp.frames):
+        f.ghost_texture = 1 + k
+    assert L.rf_batch_plan(inp.frames, len(projects), tile, rpt, ctypes.byref(z)) == RF_OK
+    assert z.ghost_textures == 1
+    inp.frames[3].ghost_texture = 0
+    assert L.rf_batch_plan(inp.frames, len(projects), tile, rpt, ctypes.byref(z)) == RF_OK
+    assert z.ghost_textures == 0
 
 
 def test_plan_rejects_bad_settings(L, projects):
