@@ -13,11 +13,18 @@ intensities and leave radii, gaps and thicknesses further from the truth than th
 The recovery therefore runs in two stages:
 
 1. coarse: per blur width in ``sigmas`` (wide to narrow), ``coarse_steps`` Adam steps on the
-   distance between the Gaussian-blurred target and the blurred splat of the traced rays
-   (``DifferentiableRenderer.splat``, the three AP1 channels), each normalised to unit sum.
-   The splat is smooth in the ray positions, so its gradient (through ``rf_trace_adjoint``)
-   moves ghosts towards where the target has them. ``views`` renders the lens at further
-   known light offsets (normalised field units) as more targets of the same unknowns;
+   distance between the Gaussian-blurred target and the blurred model (the three AP1
+   channels, each image normalised to unit sum). The splat of the traced rays
+   (``DifferentiableRenderer.splat``) is smooth in the ray positions, so its gradient
+   (through ``rf_trace_adjoint``) moves ghosts towards where the target has them. With
+   ``corrected`` (the default) the model is the blurred render with the splat's gradient:
+   blur(render) + splat - detach(splat), so the loss and its residual are the blurred
+   render's own and only the direction of descent comes from the splat; the true
+   parameters are then a stationary point, which they are not for the splat alone (the
+   blurred splat and the blurred render differ by the quads' shapes and the ghost
+   texture's variation over them). Without ``corrected`` the model is the splat.
+   ``views`` renders the lens at further known light offsets (normalised field units) as
+   more targets of the same unknowns;
 2. image: ``steps`` Adam steps on the L2 distance of the render to the target over the
    parameters in ``image_params`` (by default the coating thicknesses, which the image
    gradient determines through the reflectances; the geometry keeps the coarse stage's
@@ -67,7 +74,7 @@ def _params(base: list, z: list, offset=(0.0, 0.0)) -> list:
 def recover(project: Project, ghost: torch.Tensor, steps: int = 200, lr: float = 0.005, seed: int = 0,
             sigmas: tuple = (8.0, 4.0, 2.0, 1.0), coarse_steps: int = 100, coarse_lr: float = 0.05,
             decay: float = 0.995, views: tuple = ((0.0, 0.0),), image_params: tuple = ('thickness',),
-            accurate: bool = False) -> Recovery:
+            accurate: bool = False, corrected: bool = True) -> Recovery:
     renderer = DifferentiableRenderer(project, ghost, accurate=accurate)
     base = [t.detach() for t in renderer.params.tensors()]
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -107,8 +114,15 @@ def recover(project: Project, ghost: torch.Tensor, steps: int = 200, lr: float =
                 opt.zero_grad()
                 loss = 0.0
                 for v, tb in zip(views, tbs):
-                    sp = renderer.splat(renderer.trace(*_params(base, z, v)), sg, channels=True)
-                    loss = loss + ((sp / sp.sum() - tb) ** 2).sum() * tb.numel()
+                    pv = _params(base, z, v)
+                    sp = renderer.splat(renderer.trace(*pv), sg, channels=True)
+                    model = sp / sp.sum()
+                    if corrected:
+                        with torch.no_grad():
+                            im = renderer.render(*[q.detach() for q in pv])
+                            rb = torch.stack([gaussian_blur(im[..., c], sg) for c in range(3)])
+                        model = rb / rb.sum() + (model - model.detach())
+                    loss = loss + ((model - tb) ** 2).sum() * tb.numel()
                 loss.backward()
                 opt.step()
                 sched.step()
