@@ -382,9 +382,10 @@ int rf_bin_tiles_batch(const rf_frame* frames, const rf_batch_sizes* sizes, cons
  * lookups (no counterpart in the reference: its rasteriser reads an OpenCL image,
  * rasterizing.cl:483-485): created once per device, address and size and kept by the library.
  * *texture = 0 when the address or the row pitch (width * 4 bytes) is not aligned as the
- * device's textures require; the raster then loads the texels. rf_raster and
- * rf_raster_ordered use it by themselves; a batch passes it per frame in
- * rf_frame.ghost_texture. */
+ * device's textures require, or when the library already holds 4096 of them (it keeps
+ * every object for the life of the process and never synchronises to release one); the
+ * raster then loads the texels. rf_raster, rf_raster_ordered and rf_raster_backward use
+ * it by themselves; a batch passes it per frame in rf_frame.ghost_texture. */
 int rf_ghost_texture_object(const float* ghost, int32_t width, int32_t height, uint64_t* texture);
 
 int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* vertexes,

@@ -1190,6 +1190,7 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
 // per device, address and size and kept (a handful of descriptors; past 256 the device is
 // synchronised and the cache cleared, so no kernel can still be using one). 0 when the
 // address or the row pitch is not aligned as textures require; the raster then loads texels.
+constexpr size_t kMaxGhostTextures = 4096;
 unsigned long long ghost_texture_object(const float* ghost, int w, int h) {
     struct Entry {
         int dev;
@@ -1213,17 +1214,10 @@ unsigned long long ghost_texture_object(const float* ghost, int w, int h) {
         return 0;
     if (((size_t)w * sizeof(float)) % (size_t)pitch_align != 0 || (uintptr_t)ghost % (uintptr_t)base_align != 0)
         return 0;
-    if (cache.size() >= 256) {
-        if (cudaDeviceSynchronize() != cudaSuccess) return 0;
-        for (const Entry& e : cache) {
-            int cur = 0;
-            cudaGetDevice(&cur);
-            cudaSetDevice(e.dev);
-            cudaDestroyTextureObject(e.obj);
-            cudaSetDevice(cur);
-        }
-        cache.clear();
-    }
+    // Objects are kept for the life of the process (one per device, address and size; a
+    // kernel in flight may still use any of them, and no synchronisation is allowed here:
+    // a caller may be capturing a graph). Past the cap the raster loads the texels.
+    if (cache.size() >= kMaxGhostTextures) return 0;
     cudaResourceDesc rd = {};
     rd.resType = cudaResourceTypePitch2D;
     rd.res.pitch2D.devPtr = const_cast<float*>(ghost);

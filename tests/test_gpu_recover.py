@@ -44,7 +44,7 @@ def test_corrected_coarse_stage_is_stationary_at_the_truth(workload):
             model = tb + (model - model.detach())
         loss = ((model - tb) ** 2).sum()
         loss.backward()
-        grads[corrected] = (float(loss), torch.cat([q.grad.reshape(-1) for q in params]))
+        grads[corrected] = (float(loss.detach()), torch.cat([q.grad.reshape(-1) for q in params]))
     loss_c, g_c = grads[True]
     loss_s, g_s = grads[False]
     assert loss_c == 0.0 and float(g_c.abs().max()) == 0.0
