@@ -42,6 +42,14 @@ constexpr int kCheckpoint = RF_ADJOINT_CHECKPOINT;
 constexpr int kMaxCheckpoints = (kAdjMaxSteps + kCheckpoint - 1) / kCheckpoint;
 static_assert(kAdjMaxElements <= 128, "an element index and the reflection flag share one byte");
 constexpr int kAdjTableRows = 4;
+// consecutive rays a warp takes (a block: kAdjThreads / 32 such spans); the warp packs the
+// rays whose outputs have a gradient into full warps before tracing them back
+#ifndef RF_ADJOINT_WARP_RAYS
+#define RF_ADJOINT_WARP_RAYS 128
+#endif
+constexpr int kAdjWarpRays = RF_ADJOINT_WARP_RAYS;
+constexpr int kAdjBlockRays = kAdjThreads / 32 * kAdjWarpRays;
+static_assert(kAdjWarpRays % 32 == 0, "whole warps of rays");
 constexpr int kGradPerElement = 4;  // radius, center, coating thickness 0 and 1
 
 // ---------------------------------------------------------------- three-tangent duals
@@ -242,9 +250,10 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
     __shared__ SmemElement se[kAdjMaxElements];
     __shared__ float ior_tab[kAdjTableRows * kAdjMaxElements];
     __shared__ float acc[kAdjMaxElements * kGradPerElement + 3];
+    __shared__ int queue[kAdjThreads / 32][64];  // per warp: ray offsets (in its span) still to trace
     const int E = p.E;
-    const long long first = (long long)blockIdx.x * kAdjThreads;
-    const long long last = min(first + kAdjThreads, p.n_rays) - 1;
+    const long long first = (long long)blockIdx.x * kAdjBlockRays;
+    const long long last = min(first + kAdjBlockRays, p.n_rays) - 1;
     const long long pw_first = first / p.R, pw_last = last / p.R;
     const long long span_rows = pw_last - pw_first + 1;
     const int span = (int)(span_rows < (long long)p.W ? span_rows : (long long)p.W);
@@ -273,28 +282,9 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
     for (int i = threadIdx.x; i < E * kGradPerElement + 3; i += kAdjThreads) acc[i] = 0.0f;
     __syncthreads();
 
-    const int lane = threadIdx.x & 31;
-    // every lane runs the reverse sweep (lanes without a valid ray add zeros), so that the
-    // warp can sum each step's gradient with shuffles when its rays share one ghost path
-    // and wavelength (the same element sequence); otherwise lanes add to shared memory
-    const long long idx_raw = first + threadIdx.x;
-    const bool in_range = idx_raw < p.n_rays;
-    const long long idx = in_range ? idx_raw : first;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long n = p.n_rays;
-    const int ray_id = (int)(idx % p.R);
-    const long long pw = idx / p.R;
-    const int wl_id = (int)(pw % p.W);
-    const int path_id = (int)(pw / p.W);
-    const int row = (int)((pw - pw_first) % p.W);
-    const float* ior_row = table ? ior_tab + row * E : nullptr;
-    const float wavelength = __ldg(wavelengths + wl_id);
     const float* coef_base = &elements[0].coefficients[0];
-    auto ior_of = [&](int el) -> float {
-        if (ior_row) return ior_row[el];
-        float nn = se[el].ior;
-        if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
-        return nn;
-    };
     TraceFrame f;
     f.E = E;
     f.aperture = p.aperture;
@@ -307,6 +297,54 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
     f.dir[0] = p.dir[0];
     f.dir[1] = p.dir[1];
     f.dir[2] = p.dir[2];
+    // The warp's span of consecutive rays; rays whose outputs have no gradient (rays that
+    // miss, rays outside every covered pixel) contribute nothing and are not traced back.
+    // The others are packed in order into full warps (a queue of up to 63 offsets), so
+    // lanes are not left idle through a whole reverse sweep; rays of one span mostly share
+    // their ghost path and wavelength (R = G^2 consecutive rays do).
+    const long long span_first = first + (long long)warp * kAdjWarpRays;
+    const long long span_end = min(span_first + kAdjWarpRays, n);
+    int* q = queue[warp];
+    int queued = 0;
+    long long scan = span_first;
+    for (;;) {
+        while (queued < 32 && scan < span_end) {
+            const long long i = scan + lane;
+            bool has = false;
+            if (i < span_end)
+#pragma unroll
+                for (int k = 0; k < 6; k++) has = has || grad_rays[k * n + i] != 0.0f;
+            const unsigned m = __ballot_sync(0xffffffffu, has);
+            if (has) q[queued + __popc(m & ((1u << lane) - 1u))] = (int)(i - span_first);
+            queued += __popc(m);
+            scan += 32;
+        }
+        __syncwarp();
+        if (queued == 0) break;
+        const int take = min(queued, 32), rest = queued - take;
+        const int mine = lane < take ? q[lane] : -1;
+        const int moved = lane < rest ? q[take + lane] : 0;
+        __syncwarp();
+        if (lane < rest) q[lane] = moved;
+        queued = rest;
+    // every lane runs the reverse sweep (lanes without a valid ray add zeros), so that the
+    // warp can sum each step's gradient with shuffles when its rays share one ghost path
+    // and wavelength (the same element sequence); otherwise lanes add to shared memory
+    const bool in_range = mine >= 0;
+    const long long idx = in_range ? span_first + mine : span_first;
+    const int ray_id = (int)(idx % p.R);
+    const long long pw = idx / p.R;
+    const int wl_id = (int)(pw % p.W);
+    const int path_id = (int)(pw / p.W);
+    const int row = (int)((pw - pw_first) % p.W);
+    const float* ior_row = table ? ior_tab + row * E : nullptr;
+    const float wavelength = __ldg(wavelengths + wl_id);
+    auto ior_of = [&](int el) -> float {
+        if (ior_row) return ior_row[el];
+        float nn = se[el].ior;
+        if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
+        return nn;
+    };
     const int gy = (int)truncf((float)ray_id / (float)p.G);
     const int gx = ray_id - gy * p.G;
     // a ray whose outputs have no gradient contributes nothing: it is not re-traced
@@ -459,14 +497,21 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
             gd = gdin;
         }
         if (uniform) {
+            // the warp's four sums in one reduce-scatter: lanes exchange halves of their
+            // values (lane bit 4 picks components 2-3 or 0-1, bit 3 one of those), then sum
+            // within groups of 8; lanes 0, 8, 16, 24 end with components 0, 1, 2, 3
+            static_assert(kGradPerElement == 4, "four gradient components per element");
             el = __shfl_sync(0xffffffffu, el, leader);
-#pragma unroll
-            for (int k = 0; k < kGradPerElement; k++) {
-                float v = g4[k];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (lane == 0 && v != 0.0f) atomicAdd(&acc[el * kGradPerElement + k], v);
-            }
+            const bool hi = (lane & 16) != 0, odd = (lane & 8) != 0;
+            float a = hi ? g4[2] : g4[0], b = hi ? g4[3] : g4[1];
+            a += __shfl_xor_sync(0xffffffffu, hi ? g4[0] : g4[2], 16);
+            b += __shfl_xor_sync(0xffffffffu, hi ? g4[1] : g4[3], 16);
+            float v = odd ? b : a;
+            v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 4);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            if ((lane & 7) == 0 && v != 0.0f) atomicAdd(&acc[el * kGradPerElement + (lane >> 3)], v);
         } else if (valid && j < rec.n) {
 #pragma unroll
             for (int k = 0; k < kGradPerElement; k++)
@@ -494,6 +539,7 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
         if (lane == 0 && v != 0.0f)
             atomicAdd(&acc[k < 2 ? k : E * kGradPerElement + (k - 2)], v);
     }
+    }  // the warp's next 32 rays
     __syncthreads();
     for (int i = threadIdx.x; i < E * kGradPerElement; i += kAdjThreads)
         if (acc[i] != 0.0f) atomicAdd(&grad_elements[i], acc[i]);
@@ -521,7 +567,7 @@ extern "C" int rf_trace_adjoint(const rf_lens_element* elements, const int32_t* 
     TraceParams p;
     if (!trace_params(a, p)) return RF_ERR_INVALID_ARG;
     if (p.n_rays == 0) return RF_OK;
-    k_trace_adjoint<<<blocks_for(p.n_rays, kAdjThreads), kAdjThreads, 0, s>>>(elements, (const int2*)paths,
+    k_trace_adjoint<<<blocks_for(p.n_rays, kAdjBlockRays), kAdjThreads, 0, s>>>(elements, (const int2*)paths,
                                                                            wavelengths, p, grad_rays, grad_elements,
                                                                            grad_direction);
     return launch_status();
