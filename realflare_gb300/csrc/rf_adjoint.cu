@@ -5,7 +5,9 @@
 // rrel, reflectance), rf_trace_adjoint returns the gradient with respect to every lens
 // element's radius, center and coating thicknesses and to the (normalised) light direction.
 //
-// Per ray, the thread re-traces the ray from its entry with the forward's own code
+// Rays whose outputs carry no gradient are skipped: each warp packs the others of its span
+// of consecutive rays into full warps. Per ray, the thread re-traces the ray from its entry
+// with the forward's own code
 // (rf_trace_core.cuh, compiled like rf_trace.cu without floating-point contraction, so the
 // re-trace takes the same path). It keeps only every kCheckpoint-th step's state (position
 // and direction entering the element) and one byte per step (element, reflected or not);
@@ -327,218 +329,218 @@ __global__ void __launch_bounds__(kAdjThreads, RF_ADJOINT_MIN_BLOCKS) k_trace_ad
         __syncwarp();
         if (lane < rest) q[lane] = moved;
         queued = rest;
-    // every lane runs the reverse sweep (lanes without a valid ray add zeros), so that the
-    // warp can sum each step's gradient with shuffles when its rays share one ghost path
-    // and wavelength (the same element sequence); otherwise lanes add to shared memory
-    const bool in_range = mine >= 0;
-    const long long idx = in_range ? span_first + mine : span_first;
-    const int ray_id = (int)(idx % p.R);
-    const long long pw = idx / p.R;
-    const int wl_id = (int)(pw % p.W);
-    const int path_id = (int)(pw / p.W);
-    const int row = (int)((pw - pw_first) % p.W);
-    const float* ior_row = table ? ior_tab + row * E : nullptr;
-    const float wavelength = __ldg(wavelengths + wl_id);
-    auto ior_of = [&](int el) -> float {
-        if (ior_row) return ior_row[el];
-        float nn = se[el].ior;
-        if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
-        return nn;
-    };
-    const int gy = (int)truncf((float)ray_id / (float)p.G);
-    const int gx = ray_id - gy * p.G;
-    // a ray whose outputs have no gradient contributes nothing: it is not re-traced
-    float g_out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    bool needed = false;
-    if (in_range) {
+        // every lane runs the reverse sweep (lanes without a valid ray add zeros), so that the
+        // warp can sum each step's gradient with shuffles when its rays share one ghost path
+        // and wavelength (the same element sequence); otherwise lanes add to shared memory
+        const bool in_range = mine >= 0;
+        const long long idx = in_range ? span_first + mine : span_first;
+        const int ray_id = (int)(idx % p.R);
+        const long long pw = idx / p.R;
+        const int wl_id = (int)(pw % p.W);
+        const int path_id = (int)(pw / p.W);
+        const int row = (int)((pw - pw_first) % p.W);
+        const float* ior_row = table ? ior_tab + row * E : nullptr;
+        const float wavelength = __ldg(wavelengths + wl_id);
+        auto ior_of = [&](int el) -> float {
+            if (ior_row) return ior_row[el];
+            float nn = se[el].ior;
+            if (disperse && nn > 1.0f) nn = dispersion(wavelength, coef_base + (size_t)el * 16);
+            return nn;
+        };
+        const int gy = (int)truncf((float)ray_id / (float)p.G);
+        const int gx = ray_id - gy * p.G;
+        // a ray whose outputs have no gradient contributes nothing: it is not re-traced
+        float g_out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        bool needed = false;
+        if (in_range) {
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-            g_out[k] = grad_rays[k * n + idx];
-            needed = needed || g_out[k] != 0.0f;
-        }
-    }
-    State checkpoints[kMaxCheckpoints];
-    unsigned char tags[kAdjMaxSteps];
-    CheckpointRecorder rec{checkpoints, tags, 0, -1, 0.0f};
-    float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (needed)
-        trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
-                      f, out, rec);
-    const bool valid = needed && !isnan(out[5]) && rec.n <= kAdjMaxSteps && rec.n > 0;
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    const int leader = vmask ? __ffs(vmask) - 1 : 0;
-    const int key = path_id * p.W + wl_id;
-    const int lead_key = __shfl_sync(0xffffffffu, key, leader);  // every lane takes part
-    const bool uniform = __all_sync(0xffffffffu, !valid || key == lead_key);
-    const int n_steps = __reduce_max_sync(0xffffffffu, valid ? (unsigned)rec.n : 0u);
-    const float refl = out[5];
-    V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);  // adjoint of the state leaving a step
-    bool apt_pending = true;  // the last aperture crossing sets pos_apt
-    // the states entering the steps of the current segment, regenerated from its checkpoint
-    // by the forward's step (intersect, then reflect or refract; the stop and the sensor
-    // keep the direction)
-    State seg[kCheckpoint];
-    for (int j = n_steps - 1; j >= 0; j--) {
-        if (j == n_steps - 1 || (j + 1) % kCheckpoint == 0) {
-            const int j0 = j - j % kCheckpoint;
-            if (valid && j0 < rec.n) {
-                State st = checkpoints[j0 / kCheckpoint];
-                const int j1 = min(j + 1, rec.n);
-                for (int q = j0; q < j1; q++) {
-                    seg[q - j0] = st;
-                    if (q + 1 == j1) break;
-                    const int i = tags[q] & 0x7f;
-                    const Hit h = intersect(st.px, st.py, st.pz, st.dx, st.dy, st.dz, se[i]);
-                    const State in = st;
-                    st.px = h.px;
-                    st.py = h.py;
-                    st.pz = h.pz;
-                    if (i == p.aperture || i == E - 1) continue;
-                    const int n_index = (in.dz < 0.0f) ? i - 1 : i + 1;
-                    if (tags[q] & 0x80) {
-                        reflect_dir(st.dx, st.dy, st.dz, h);
-                    } else {
-                        const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
-                        refract_dir(st.dx, st.dy, st.dz, h, n1, ior_of(i));
-                    }
-                }
+            for (int k = 0; k < 6; k++) {
+                g_out[k] = grad_rays[k * n + idx];
+                needed = needed || g_out[k] != 0.0f;
             }
         }
-        float g4[kGradPerElement] = {0.f, 0.f, 0.f, 0.f};
-        int el = 0;
-        if (valid && j < rec.n) {
-            const State& st = seg[j % kCheckpoint];
-            const int tag = tags[j];
-            const int i = tag & 0x7f;
-            el = i;
-            const SmemElement& e = se[i];
-            const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
-            const Hit h = intersect(pin.x, pin.y, pin.z, din.x, din.y, din.z, e);
-            V3 gh = gp;  // adjoint of the hit point
-            V3 gn = v3(0.0f, 0.0f, 0.0f);
-            V3 gdin = v3(0.0f, 0.0f, 0.0f);
-            if (j == rec.n - 1) gh = gh + v3(g_out[0], g_out[1], 0.0f);  // sensor position
-            if (i == p.aperture) {
-                if (apt_pending) {
-                    gh.x += g_out[2] / e.height;
-                    gh.y += g_out[3] / e.height;
-                    apt_pending = false;
-                }
-                gdin = gd;  // no change of direction at the stop
-            } else {
-                if (j == rec.argmax) {
-                    const float rxy = sqrtf(h.px * h.px + h.py * h.py);
-                    if (rxy > 0.0f) {
-                        const float sc = g_out[4] / (rxy * e.height);
-                        gh.x += sc * h.px;
-                        gh.y += sc * h.py;
-                    }
-                }
-                const V3 nrm = v3(h.nx, h.ny, h.nz);
-                if (i == E - 1) {
-                    gdin = gd;
-                } else {
-                    const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
-                    const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
-                    const float n2 = ior_of(i);
-                    if (tag & 0x80) {
-                        // d' = d - 2 (d.n) n
-                        const float dn = dot(din, nrm), gdn = dot(gd, nrm);
-                        gdin = gd - nrm * (2.0f * gdn);
-                        gn = gn - (gd * dn + din * gdn) * 2.0f;
-                        // reflectance factor R(theta, thicknesses), refl *= R when R > 0
-                        const float c = -dn;
-                        const float cc = clampf(c, -1.0f, 1.0f);
-                        const float incident = acosf(cc);
-                        const float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
-                        D3 th = {theta, 1.0f, 0.0f, 0.0f};
-                        D3 R;
-                        float gtheta = 0.0f;
-                        if (e.layers == 2) {
-                            R = fresnel_two_layer_d(th, wavelength, n1, p.layer_n0, D3{e.d0, 0.f, 1.f, 0.f},
-                                                    p.layer_n1, D3{e.d1, 0.f, 0.f, 1.f}, n2);
-                        } else if (e.layers == 1 || e.coating > 0) {
-                            const float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
-                            const D3 d1 = e.layers == 1 ? D3{e.d0, 0.f, 1.f, 0.f}
-                                                        : dconst((float)e.coating / (4.0f * nc));
-                            R = fresnel_ar_d(th, wavelength, d1, n1, nc, n2);
+        State checkpoints[kMaxCheckpoints];
+        unsigned char tags[kAdjMaxSteps];
+        CheckpointRecorder rec{checkpoints, tags, 0, -1, 0.0f};
+        float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (needed)
+            trace_ray_rec(se, ior_row, disperse, coef_base, wavelength, __ldg(paths + path_id), p.grid[gx], p.grid[gy],
+                          f, out, rec);
+        const bool valid = needed && !isnan(out[5]) && rec.n <= kAdjMaxSteps && rec.n > 0;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        const int leader = vmask ? __ffs(vmask) - 1 : 0;
+        const int key = path_id * p.W + wl_id;
+        const int lead_key = __shfl_sync(0xffffffffu, key, leader);  // every lane takes part
+        const bool uniform = __all_sync(0xffffffffu, !valid || key == lead_key);
+        const int n_steps = __reduce_max_sync(0xffffffffu, valid ? (unsigned)rec.n : 0u);
+        const float refl = out[5];
+        V3 gp = v3(0.0f, 0.0f, 0.0f), gd = v3(0.0f, 0.0f, 0.0f);  // adjoint of the state leaving a step
+        bool apt_pending = true;  // the last aperture crossing sets pos_apt
+        // the states entering the steps of the current segment, regenerated from its checkpoint
+        // by the forward's step (intersect, then reflect or refract; the stop and the sensor
+        // keep the direction)
+        State seg[kCheckpoint];
+        for (int j = n_steps - 1; j >= 0; j--) {
+            if (j == n_steps - 1 || (j + 1) % kCheckpoint == 0) {
+                const int j0 = j - j % kCheckpoint;
+                if (valid && j0 < rec.n) {
+                    State st = checkpoints[j0 / kCheckpoint];
+                    const int j1 = min(j + 1, rec.n);
+                    for (int q = j0; q < j1; q++) {
+                        seg[q - j0] = st;
+                        if (q + 1 == j1) break;
+                        const int i = tags[q] & 0x7f;
+                        const Hit h = intersect(st.px, st.py, st.pz, st.dx, st.dy, st.dz, se[i]);
+                        const State in = st;
+                        st.px = h.px;
+                        st.py = h.py;
+                        st.pz = h.pz;
+                        if (i == p.aperture || i == E - 1) continue;
+                        const int n_index = (in.dz < 0.0f) ? i - 1 : i + 1;
+                        if (tags[q] & 0x80) {
+                            reflect_dir(st.dx, st.dy, st.dz, h);
                         } else {
-                            R = fresnel_d(th, n1, n2);
+                            const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
+                            refract_dir(st.dx, st.dy, st.dz, h, n1, ior_of(i));
                         }
-                        if (R.v > 0.0f) {
-                            const float gR = g_out[5] * refl / R.v;
-                            gtheta = gR * R.g0;
-                            g4[2] += gR * R.g1;
-                            g4[3] += gR * R.g2;
-                        }
-                        if (fabsf(c) < 1.0f) {
-                            const float gc = gtheta * (-rsqrtf(1.0f - c * c));
-                            // c = -d.n
-                            gdin = gdin - nrm * gc;
-                            gn = gn - din * gc;
-                        }
-                    } else {
-                        // d' = o d + k n, k = o c - sqrt(1 - o^2 (1 - c^2)), c = -d.n
-                        const float o = n1 / n2;
-                        const float c = -dot(din, nrm);
-                        const float sint2 = (o * o) * (1.0f - c * c);
-                        const float sq = sqrtf(fabsf(1.0f - sint2));
-                        const float k = o * c - sq;
-                        const float gk = dot(gd, nrm);
-                        const float dk_dc = sq > 0.0f ? o - o * o * c / sq : o;
-                        gdin = gd * o - nrm * (gk * dk_dc);
-                        gn = gn + gd * k - din * (gk * dk_dc);
                     }
                 }
             }
-            V3 gpin = v3(0.0f, 0.0f, 0.0f);
-            intersect_adjoint(pin, din, e, gh, gn, gpin, gdin, g4[0], g4[1]);
-            gp = gpin;
-            gd = gdin;
-        }
-        if (uniform) {
-            // the warp's four sums in one reduce-scatter: lanes exchange halves of their
-            // values (lane bit 4 picks components 2-3 or 0-1, bit 3 one of those), then sum
-            // within groups of 8; lanes 0, 8, 16, 24 end with components 0, 1, 2, 3
-            static_assert(kGradPerElement == 4, "four gradient components per element");
-            el = __shfl_sync(0xffffffffu, el, leader);
-            const bool hi = (lane & 16) != 0, odd = (lane & 8) != 0;
-            float a = hi ? g4[2] : g4[0], b = hi ? g4[3] : g4[1];
-            a += __shfl_xor_sync(0xffffffffu, hi ? g4[0] : g4[2], 16);
-            b += __shfl_xor_sync(0xffffffffu, hi ? g4[1] : g4[3], 16);
-            float v = odd ? b : a;
-            v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 8);
-            v += __shfl_xor_sync(0xffffffffu, v, 4);
-            v += __shfl_xor_sync(0xffffffffu, v, 2);
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            if ((lane & 7) == 0 && v != 0.0f) atomicAdd(&acc[el * kGradPerElement + (lane >> 3)], v);
-        } else if (valid && j < rec.n) {
+            float g4[kGradPerElement] = {0.f, 0.f, 0.f, 0.f};
+            int el = 0;
+            if (valid && j < rec.n) {
+                const State& st = seg[j % kCheckpoint];
+                const int tag = tags[j];
+                const int i = tag & 0x7f;
+                el = i;
+                const SmemElement& e = se[i];
+                const V3 pin = v3(st.px, st.py, st.pz), din = v3(st.dx, st.dy, st.dz);
+                const Hit h = intersect(pin.x, pin.y, pin.z, din.x, din.y, din.z, e);
+                V3 gh = gp;  // adjoint of the hit point
+                V3 gn = v3(0.0f, 0.0f, 0.0f);
+                V3 gdin = v3(0.0f, 0.0f, 0.0f);
+                if (j == rec.n - 1) gh = gh + v3(g_out[0], g_out[1], 0.0f);  // sensor position
+                if (i == p.aperture) {
+                    if (apt_pending) {
+                        gh.x += g_out[2] / e.height;
+                        gh.y += g_out[3] / e.height;
+                        apt_pending = false;
+                    }
+                    gdin = gd;  // no change of direction at the stop
+                } else {
+                    if (j == rec.argmax) {
+                        const float rxy = sqrtf(h.px * h.px + h.py * h.py);
+                        if (rxy > 0.0f) {
+                            const float sc = g_out[4] / (rxy * e.height);
+                            gh.x += sc * h.px;
+                            gh.y += sc * h.py;
+                        }
+                    }
+                    const V3 nrm = v3(h.nx, h.ny, h.nz);
+                    if (i == E - 1) {
+                        gdin = gd;
+                    } else {
+                        const int n_index = (din.z < 0.0f) ? i - 1 : i + 1;
+                        const float n1 = (0 <= n_index && n_index < E) ? ior_of(n_index) : 1.0f;
+                        const float n2 = ior_of(i);
+                        if (tag & 0x80) {
+                            // d' = d - 2 (d.n) n
+                            const float dn = dot(din, nrm), gdn = dot(gd, nrm);
+                            gdin = gd - nrm * (2.0f * gdn);
+                            gn = gn - (gd * dn + din * gdn) * 2.0f;
+                            // reflectance factor R(theta, thicknesses), refl *= R when R > 0
+                            const float c = -dn;
+                            const float cc = clampf(c, -1.0f, 1.0f);
+                            const float incident = acosf(cc);
+                            const float theta = incident < 0.02f ? (float)((double)incident + 1e-9) : incident;
+                            D3 th = {theta, 1.0f, 0.0f, 0.0f};
+                            D3 R;
+                            float gtheta = 0.0f;
+                            if (e.layers == 2) {
+                                R = fresnel_two_layer_d(th, wavelength, n1, p.layer_n0, D3{e.d0, 0.f, 1.f, 0.f},
+                                                        p.layer_n1, D3{e.d1, 0.f, 0.f, 1.f}, n2);
+                            } else if (e.layers == 1 || e.coating > 0) {
+                                const float nc = fmaxf(sqrtf(n1 * n2), p.cmin);
+                                const D3 d1 = e.layers == 1 ? D3{e.d0, 0.f, 1.f, 0.f}
+                                                            : dconst((float)e.coating / (4.0f * nc));
+                                R = fresnel_ar_d(th, wavelength, d1, n1, nc, n2);
+                            } else {
+                                R = fresnel_d(th, n1, n2);
+                            }
+                            if (R.v > 0.0f) {
+                                const float gR = g_out[5] * refl / R.v;
+                                gtheta = gR * R.g0;
+                                g4[2] += gR * R.g1;
+                                g4[3] += gR * R.g2;
+                            }
+                            if (fabsf(c) < 1.0f) {
+                                const float gc = gtheta * (-rsqrtf(1.0f - c * c));
+                                // c = -d.n
+                                gdin = gdin - nrm * gc;
+                                gn = gn - din * gc;
+                            }
+                        } else {
+                            // d' = o d + k n, k = o c - sqrt(1 - o^2 (1 - c^2)), c = -d.n
+                            const float o = n1 / n2;
+                            const float c = -dot(din, nrm);
+                            const float sint2 = (o * o) * (1.0f - c * c);
+                            const float sq = sqrtf(fabsf(1.0f - sint2));
+                            const float k = o * c - sq;
+                            const float gk = dot(gd, nrm);
+                            const float dk_dc = sq > 0.0f ? o - o * o * c / sq : o;
+                            gdin = gd * o - nrm * (gk * dk_dc);
+                            gn = gn + gd * k - din * (gk * dk_dc);
+                        }
+                    }
+                }
+                V3 gpin = v3(0.0f, 0.0f, 0.0f);
+                intersect_adjoint(pin, din, e, gh, gn, gpin, gdin, g4[0], g4[1]);
+                gp = gpin;
+                gd = gdin;
+            }
+            if (uniform) {
+                // the warp's four sums in one reduce-scatter: lanes exchange halves of their
+                // values (lane bit 4 picks components 2-3 or 0-1, bit 3 one of those), then sum
+                // within groups of 8; lanes 0, 8, 16, 24 end with components 0, 1, 2, 3
+                static_assert(kGradPerElement == 4, "four gradient components per element");
+                el = __shfl_sync(0xffffffffu, el, leader);
+                const bool hi = (lane & 16) != 0, odd = (lane & 8) != 0;
+                float a = hi ? g4[2] : g4[0], b = hi ? g4[3] : g4[1];
+                a += __shfl_xor_sync(0xffffffffu, hi ? g4[0] : g4[2], 16);
+                b += __shfl_xor_sync(0xffffffffu, hi ? g4[1] : g4[3], 16);
+                float v = odd ? b : a;
+                v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 8);
+                v += __shfl_xor_sync(0xffffffffu, v, 4);
+                v += __shfl_xor_sync(0xffffffffu, v, 2);
+                v += __shfl_xor_sync(0xffffffffu, v, 1);
+                if ((lane & 7) == 0 && v != 0.0f) atomicAdd(&acc[el * kGradPerElement + (lane >> 3)], v);
+            } else if (valid && j < rec.n) {
 #pragma unroll
-            for (int k = 0; k < kGradPerElement; k++)
-                if (g4[k] != 0.0f) atomicAdd(&acc[el * kGradPerElement + k], g4[k]);
+                for (int k = 0; k < kGradPerElement; k++)
+                    if (g4[k] != 0.0f) atomicAdd(&acc[el * kGradPerElement + k], g4[k]);
+            }
         }
-    }
-    // entry ray: p_in = hit0 - dir, d_in = dir; hit0 = grid point hitting element 0
-    V3 gdir = v3(0.0f, 0.0f, 0.0f);
-    float g0r = 0.0f, g0c = 0.0f;
-    if (valid) {
-        gdir = gd - gp;
-        const V3 g0 = v3(p.grid[gx], -p.grid[gy], 1.0f);
-        const Hit h0 = intersect(g0.x, g0.y, g0.z, 0.0f, 0.0f, -1.0f, se[0]);
-        if (h0.hit) {
-            V3 gpg = v3(0.f, 0.f, 0.f), gdg = v3(0.f, 0.f, 0.f);
-            intersect_adjoint(g0, v3(0.0f, 0.0f, -1.0f), se[0], gp, v3(0.f, 0.f, 0.f), gpg, gdg, g0r, g0c);
+        // entry ray: p_in = hit0 - dir, d_in = dir; hit0 = grid point hitting element 0
+        V3 gdir = v3(0.0f, 0.0f, 0.0f);
+        float g0r = 0.0f, g0c = 0.0f;
+        if (valid) {
+            gdir = gd - gp;
+            const V3 g0 = v3(p.grid[gx], -p.grid[gy], 1.0f);
+            const Hit h0 = intersect(g0.x, g0.y, g0.z, 0.0f, 0.0f, -1.0f, se[0]);
+            if (h0.hit) {
+                V3 gpg = v3(0.f, 0.f, 0.f), gdg = v3(0.f, 0.f, 0.f);
+                intersect_adjoint(g0, v3(0.0f, 0.0f, -1.0f), se[0], gp, v3(0.f, 0.f, 0.f), gpg, gdg, g0r, g0c);
+            }
         }
-    }
-    const float tail[5] = {g0r, g0c, gdir.x, gdir.y, gdir.z};
+        const float tail[5] = {g0r, g0c, gdir.x, gdir.y, gdir.z};
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-        float v = tail[k];
+        for (int k = 0; k < 5; k++) {
+            float v = tail[k];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && v != 0.0f)
-            atomicAdd(&acc[k < 2 ? k : E * kGradPerElement + (k - 2)], v);
-    }
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && v != 0.0f)
+                atomicAdd(&acc[k < 2 ? k : E * kGradPerElement + (k - 2)], v);
+        }
     }  // the warp's next 32 rays
     __syncthreads();
     for (int i = threadIdx.x; i < E * kGradPerElement; i += kAdjThreads)
