@@ -21,6 +21,18 @@
 // Rays that do not reach the sensor have no outputs and no gradient; the discrete choices
 // (which element is hit, reflection or refraction, the rrel maximum) are those of the
 // forward, i.e. the gradient is the derivative wherever they do not change.
+// RF_ADJOINT_CALLS 1: the forward Fresnel variants out of line (the kernel's instruction
+// fetches stall it more than anything else; 7.48 against 7.51 ms per forward+adjoint on the
+// 16-surface differentiable workload); 2: the intersection too (7.54 ms)
+#ifndef RF_ADJOINT_CALLS
+#define RF_ADJOINT_CALLS 1
+#endif
+#if RF_ADJOINT_CALLS >= 1
+#define RF_CORE_COLD __noinline__
+#endif
+#if RF_ADJOINT_CALLS >= 2
+#define RF_CORE_HOT __noinline__
+#endif
 #include "rf_trace_core.cuh"
 
 namespace rf {

@@ -38,7 +38,16 @@ struct Hit {
     bool hit;
 };
 
-__device__ __forceinline__ Hit intersect(float px, float py, float pz, float dx, float dy, float dz,
+// Inlining of the reflection-only functions (RF_CORE_COLD: the Fresnel variants) and of the
+// sphere/plane intersection (RF_CORE_HOT); a unit may define them __noinline__ before
+// including this file (same arithmetic either way: nothing is contracted across calls).
+#ifndef RF_CORE_COLD
+#define RF_CORE_COLD __forceinline__
+#endif
+#ifndef RF_CORE_HOT
+#define RF_CORE_HOT __forceinline__
+#endif
+__device__ RF_CORE_HOT Hit intersect(float px, float py, float pz, float dx, float dy, float dz,
                                          const SmemElement& e) {
     Hit h;
     h.px = h.py = h.pz = h.nx = h.ny = h.nz = h.incident = 0.0f;
@@ -84,7 +93,7 @@ __device__ __forceinline__ float incident_angle(float dx, float dy, float dz, co
     return acosf(clampf(c, -1.0f, 1.0f));
 }
 
-__device__ __forceinline__ float fresnel(float theta0, float n1, float n2) {
+__device__ RF_CORE_COLD float fresnel(float theta0, float n1, float n2) {
     float theta1 = asinf(sinf(theta0) * n1 / n2);
     float cosi = cosf(theta0);
     float cost = cosf(theta1);
@@ -93,7 +102,7 @@ __device__ __forceinline__ float fresnel(float theta0, float n1, float n2) {
     return (rs * rs + rp * rp) / 2.0f;
 }
 
-__device__ __forceinline__ float fresnel_ar(float theta0, float lambda, float d1, float n0, float n1, float n2) {
+__device__ RF_CORE_COLD float fresnel_ar(float theta0, float lambda, float d1, float n0, float n1, float n2) {
     float s0 = sinf(theta0);
     float theta1 = asinf(s0 * n0 / n1);
     float theta2 = asinf(s0 * n0 / n2);
@@ -135,7 +144,7 @@ __device__ __forceinline__ float stack_r2(float r01, float r12, float r23, float
     float bre = 1.0f + r01 * ere, bim = r01 * eim;
     return (tre * tre + tim * tim) / (bre * bre + bim * bim);
 }
-__device__ __forceinline__ float fresnel_two_layer(float theta0, float lambda, float n0, float na, float da,
+__device__ RF_CORE_COLD float fresnel_two_layer(float theta0, float lambda, float n0, float na, float da,
                                                    float nb, float db, float n2) {
     float s0, c0;
     sincosf(theta0, &s0, &c0);
