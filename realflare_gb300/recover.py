@@ -71,7 +71,7 @@ def _params(base: list, z: list, offset=(0.0, 0.0)) -> list:
     return [r0 * (1 + SCALE['radii'] * zr), g0 * (1 + SCALE['gaps'] * zg), t0 + SCALE['thickness'] * zt, light]
 
 
-def recover(project: Project, ghost: torch.Tensor, steps: int = 200, lr: float = 0.005, seed: int = 0,
+def recover(project: Project, ghost: torch.Tensor, steps: int = 200, lr: float = 0.001, seed: int = 0,
             sigmas: tuple = (8.0, 4.0, 2.0, 1.0), coarse_steps: int = 100, coarse_lr: float = 0.05,
             decay: float = 0.995, views: tuple = ((0.0, 0.0),), image_params: tuple = ('thickness',),
             accurate: bool = False, corrected: bool = True) -> Recovery:
