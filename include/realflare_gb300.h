@@ -388,6 +388,12 @@ int rf_bin_tiles_batch(const rf_frame* frames, const rf_batch_sizes* sizes, cons
  * it by themselves; a batch passes it per frame in rf_frame.ghost_texture. */
 int rf_ghost_texture_object(const float* ghost, int32_t width, int32_t height, uint64_t* texture);
 
+/* Forgets the library's ghost texture objects on the current device without destroying
+ * them: for a host that reset the device (cudaDeviceReset ends the objects with the
+ * context, and a later raster call must not be handed one of them). Call it after the reset
+ * and before the next raster call; no CUDA work is issued. */
+int rf_ghost_textures_forget(void);
+
 int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* sizes, const float* vertexes,
                     const uint32_t* tile_offsets, const uint32_t* tile_entries, const float* ghosts,
                     const float* spectrum, void* workspace, size_t workspace_bytes,

@@ -181,6 +181,7 @@ SIGNATURES = {
     'rf_batch_workspace_size': [ctypes.POINTER(BatchSizes), I64, ctypes.POINTER(ctypes.c_size_t)],
     'rf_bin_tiles_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, ctypes.c_size_t, P, P, I64, P, P],
     'rf_ghost_texture_object': [P, I32, I32, ctypes.POINTER(ctypes.c_uint64)],
+    'rf_ghost_textures_forget': [],
     'rf_raster_batch': [P, ctypes.POINTER(BatchSizes), P, P, P, P, P, P, ctypes.c_size_t, I64, P, P, P],
 }
 

@@ -1191,15 +1191,19 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
 // synchronised and the cache cleared, so no kernel can still be using one). 0 when the
 // address or the row pitch is not aligned as textures require; the raster then loads texels.
 constexpr size_t kMaxGhostTextures = 4096;
+struct GhostTextureEntry {
+    int dev;
+    const float* ptr;
+    int w, h;
+    cudaTextureObject_t obj;
+};
+std::mutex ghost_texture_mutex;
+std::vector<GhostTextureEntry> ghost_texture_cache;
+
 unsigned long long ghost_texture_object(const float* ghost, int w, int h) {
-    struct Entry {
-        int dev;
-        const float* ptr;
-        int w, h;
-        cudaTextureObject_t obj;
-    };
-    static std::mutex mutex;
-    static std::vector<Entry> cache;
+    using Entry = GhostTextureEntry;
+    std::mutex& mutex = ghost_texture_mutex;
+    std::vector<Entry>& cache = ghost_texture_cache;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     std::lock_guard<std::mutex> lock(mutex);
@@ -1333,6 +1337,19 @@ extern "C" int rf_raster_batch(const rf_frame* frames, const rf_batch_sizes* siz
         default:
             return RF_ERR_NOT_SUPPORTED;
     }
+}
+
+extern "C" int rf_ghost_textures_forget(void) {
+    using namespace rf;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return RF_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(ghost_texture_mutex);
+    auto& c = ghost_texture_cache;
+    c.erase(std::remove_if(c.begin(), c.end(), [dev](const GhostTextureEntry& e) { return e.dev == dev; }), c.end());
+    return RF_OK;
 }
 
 extern "C" int rf_ghost_texture_object(const float* ghost, int32_t width, int32_t height, uint64_t* texture) {

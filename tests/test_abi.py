@@ -47,3 +47,18 @@ def test_no_cpu_fallback_without_gpu():
 
     with pytest.raises(RealflareError):
         RaytracingTask()
+
+
+def test_host_only_calls_without_a_gpu():
+    """Calls that issue no CUDA work answer without a device: the texture cache reset reports
+    the missing device instead of touching it."""
+    torch = pytest.importorskip('torch')
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    from realflare_gb300 import build
+    from realflare_gb300._abi import RF_ERR_CUDA
+
+    if not os.path.exists(build.LIB):
+        build.build()
+    lib = ctypes.CDLL(build.LIB)
+    assert lib.rf_ghost_textures_forget() == RF_ERR_CUDA

@@ -45,6 +45,10 @@ def test_texture_objects():
     assert texture_object(shifted, 64, 64) == 0  # base address not aligned: loads
     odd = torch.zeros(75 * 64, device='cuda')
     assert texture_object(odd, 75, 64) == 0  # row pitch 300 bytes: loads
+    # after the cache is forgotten (as after a device reset) the next call makes a new object
+    assert lib().rf_ghost_textures_forget() == 0
+    h2 = texture_object(g, 64, 64)
+    assert h2 not in (0, h) and texture_object(g, 64, 64) == h2
     out = ctypes.c_uint64()
     assert lib().rf_ghost_texture_object(None, 64, 64, ctypes.byref(out)) == RF_ERR_INVALID_ARG
     assert lib().rf_ghost_texture_object(g.data_ptr(), 0, 64, ctypes.byref(out)) == RF_ERR_INVALID_ARG
