@@ -797,8 +797,8 @@ __device__ __constant__ static const int kGradSlot[kGradAttrs] = {2, 3, 4, 5, 6}
 // Backward of k_raster (32 x 32 or 16 x 16 tiles): the same tiles, entry lists, records, coverage
 // and mean-value weights as the forward (held fixed: they are piecewise constant in the
 // vertex positions), differentiating each fragment with respect to the attributes its
-// corners interpolate. Per record the warp sums its pixels' contributions with shuffles;
-// the CTA sums warps in shared memory and adds each record's totals to the two vertices
+// corners interpolate. Per record the warp sums its pixels' contributions through a
+// shared-memory transpose; the CTA sums warps in shared memory and adds each record's totals to the two vertices
 // (wavelength pair endpoints) of each corner once per tile. kTex: the ghost lookups gather
 // from the texture object p.ghost_tex.
 template <int T, int kS, bool kTex>
@@ -1187,9 +1187,9 @@ int allow_smem(K kernel, size_t bytes, std::atomic<size_t>* allowed) {
 
 // A texture object over a caller's ghost texture (float texels, pitch w * 4 bytes, border
 // address mode, point filtering, unnormalised coordinates) for ghost_sample_tex, created once
-// per device, address and size and kept (a handful of descriptors; past 256 the device is
-// synchronised and the cache cleared, so no kernel can still be using one). 0 when the
-// address or the row pitch is not aligned as textures require; the raster then loads texels.
+// per device, address and size and kept (at most kMaxGhostTextures; rf_ghost_textures_forget
+// drops a device's objects after a device reset). 0 when the address or the row pitch is not
+// aligned as textures require, or past the cap; the raster then loads texels.
 constexpr size_t kMaxGhostTextures = 4096;
 struct GhostTextureEntry {
     int dev;
