@@ -28,7 +28,8 @@ The recovery therefore runs in two stages:
 2. image: ``steps`` Adam steps on the L2 distance of the render to the target over the
    parameters in ``image_params`` (by default the coating thicknesses, which the image
    gradient determines through the reflectances; the geometry keeps the coarse stage's
-   values).
+   values), at learning rate ``lr`` (0.001: larger steps move the thicknesses to explain
+   the residuals the geometry leaves, and the parameter error rises again).
 """
 from __future__ import annotations
 
