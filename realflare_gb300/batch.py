@@ -36,9 +36,15 @@ def _ghost_key(project: Project) -> tuple:
     return (repr(f.ghost_aperture), f.ghost.fstop, r.ghost.resolution.width(), r.ghost.resolution.height())
 
 
+# ghost texture starts in the batch buffer: multiples of 128 floats (512 bytes, the texture
+# base alignment of current GPUs), so that every texture can get a texture object
+GHOST_ALIGN_FLOATS = 128
+
+
 def ghost_textures(projects: list, stream=None) -> tuple:
     """Ghost textures of the distinct ghost settings among the projects: (one float tensor of
-    all textures, per-project float offset, per-project (height, width))."""
+    all textures, per-project float offset, per-project (height, width)). Each texture starts
+    at a multiple of ``GHOST_ALIGN_FLOATS`` floats (zeros fill the gaps)."""
     from .tasks import GhostApertureTask, GhostTask
 
     aperture_task, ghost_task = GhostApertureTask(stream), GhostTask(stream)
@@ -49,6 +55,10 @@ def ghost_textures(projects: list, stream=None) -> tuple:
         key = _ghost_key(p)
         if key not in cache:
             t = ghost_task.run(p, aperture_task.run(p)).tensor
+            pad = -total % GHOST_ALIGN_FLOATS
+            if pad:
+                textures.append(torch.zeros(pad, dtype=t.dtype, device=t.device))
+                total += pad
             cache[key] = (total, tuple(t.shape[:2]))
             textures.append(t.reshape(-1))
             total += t.numel()
